@@ -1,0 +1,477 @@
+// C ABI of libeqc (include/eqc.h): model upload, reference-numbering <-> layout
+// permutation, host-array entry points.
+#include "model.h"
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+
+namespace eqc {
+
+Handle::~Handle() {
+    mg_destroy(*this);
+    if (h_ctrl) cudaFreeHost(h_ctrl);
+    if (h_scal) cudaFreeHost(h_scal);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+static void fail_if(bool cond, const std::string& msg) {
+    if (cond) throw Error(EQC_E_ARG, msg);
+}
+
+// Diagonal of K in the layout (Kassemble.jl:50-58 with i=k, j=l).
+static std::vector<double> diag_K(const Handle& h, const double* W) {
+    const Layout& L = h.L;
+    std::vector<double> dg(L.size(), 0.0);
+    const double* H = h.H;
+    for (int ey = 0; ey < L.NelY; ++ey)
+        for (int ex = 0; ex < L.NelX; ++ex) {
+            const double* w = W + ((int64_t)ey * L.NelX + ex) * 25;
+            for (int j = 0; j < 5; ++j)
+                for (int i = 0; i < 5; ++i) {
+                    double t1 = 0, t2 = 0;
+                    for (int p = 0; p < 5; ++p) {
+                        t1 += w[i + 5 * p] * h.c2 * H[j + 5 * p] * H[j + 5 * p];
+                        t2 += w[p + 5 * j] * h.c1 * H[i + 5 * p] * H[i + 5 * p];
+                    }
+                    dg[(int64_t)(4 * ey + j) * L.ld + 4 * ex + i] += t1 + t2;
+                }
+        }
+    return dg;
+}
+
+static void create(Handle& h, const eqc_model& m) {
+    fail_if(m.NGLL != 5, "NGLL must be 5");
+    fail_if(m.NelX < 1 || m.NelY < 1 || m.Nel != m.NelX * m.NelY, "Nel != NelX*NelY");
+    fail_if(m.FltNglob != 4 * m.NelX + 1, "FltNglob != 4*NelX+1");
+    fail_if(m.nglob != (4 * m.NelX + 1) * (4 * m.NelY + 1), "nglob != (4NelX+1)(4NelY+1)");
+    fail_if(!m.iglob || !m.W || !m.H || !m.M || !m.iFlt, "null model array");
+    fail_if(m.IDstate != 2, "only IDstate = 2 (aging law, log form) is on the hot path");
+    fail_if(m.ETA != 0.0, "Kelvin-Voigt damping (ETA != 0) is not on the hot path");
+    EQC_CUDA(cudaSetDevice(h.opt.device));
+    EQC_CUDA(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+    cudaStream_t s = h.stream;
+    Layout& L = h.L;
+    L.NelX = (int)m.NelX;
+    L.NelY = (int)m.NelY;
+    L.nx = 4 * L.NelX + 1;
+    L.ny = 4 * L.NelY + 1;
+    L.ld = L.nx;
+    h.nglob = m.nglob;
+    h.Nel = m.Nel;
+    h.dxe = m.dxe;
+    h.dye = m.dye;
+    const double dx_dxi = 0.5 * m.dxe, dy_deta = 0.5 * m.dye, jac = dx_dxi * dy_deta;
+    h.c1 = jac / (dx_dxi * dx_dxi);
+    h.c2 = jac / (dy_deta * dy_deta);
+    h.Vpl = m.Vpl;
+    h.Vthres = m.Vthres;
+    h.Vevne = m.Vevne;
+    h.dt0 = m.dt0;
+    h.Total_time = m.Total_time;
+    h.yr2sec = (double)m.yr2sec;
+    std::memcpy(h.H, m.H, sizeof(h.H));
+    set_H(h.H, s);
+
+    // reference node -> layout index, from the connectivity
+    h.ref2lay.assign(m.nglob, -1);
+    for (int64_t e = 0; e < m.Nel; ++e) {
+        const int ex = (int)(e % m.NelX), ey = (int)(e / m.NelX);
+        for (int j = 0; j < 5; ++j)
+            for (int i = 0; i < 5; ++i) {
+                const int64_t ref = m.iglob[i + 5 * j + 25 * e] - 1;
+                fail_if(ref < 0 || ref >= m.nglob, "iglob entry out of range");
+                const int64_t lay = (int64_t)(4 * ey + j) * L.ld + 4 * ex + i;
+                fail_if(h.ref2lay[ref] >= 0 && h.ref2lay[ref] != lay, "iglob is not a structured box mesh");
+                h.ref2lay[ref] = lay;
+            }
+    }
+    for (int64_t g = 0; g < m.nglob; ++g) fail_if(h.ref2lay[g] < 0, "iglob does not cover every node");
+    const int Nf = (int)m.FltNglob;
+    for (int k = 0; k < Nf; ++k)
+        fail_if(h.ref2lay[m.iFlt[k] - 1] != k, "iFlt must run along the y = 0 edge from x = -LX (BoundaryMatrix 'B')");
+
+    // element data
+    const size_t nW = (size_t)25 * m.Nel;
+    h.W64.alloc(nW);
+    h.W64.upload(m.W, nW, s);
+    std::vector<float> w32(nW);
+    for (size_t k = 0; k < nW; ++k) w32[k] = (float)m.W[k];
+    h.W32.alloc(nW);
+    h.W32.upload(w32.data(), nW, s);
+
+    // node arrays
+    const int64_t N = L.size();
+    std::vector<double> Mlay(N, 1.0);
+    for (int64_t g = 0; g < m.nglob; ++g) Mlay[h.ref2lay[g]] = m.M[g];
+    for (DBuf<double>* b : {&h.M, &h.d, &h.v, &h.a, &h.dPre, &h.tmp64a, &h.tmp64b, &h.r64, &h.z64, &h.p64, &h.q64})
+        b->alloc(N);
+    for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32}) b->alloc(N);
+    h.M.upload(Mlay.data(), N, s);
+    std::vector<double> dg = diag_K(h, m.W);
+    for (int64_t i = 0; i < L.ld; ++i) dg[i] = 1.0;  // fault row is not part of the system
+    std::vector<float> dg32(dg.begin(), dg.end());
+    h.diag64.alloc(N);
+    h.diag64.upload(dg.data(), N, s);
+    h.diag32.alloc(N);
+    h.diag32.upload(dg32.data(), N, s);
+
+    // boundary lists
+    auto to_lay = [&](const int64_t* idx, int64_t n) {
+        std::vector<int64_t> o(n);
+        for (int64_t k = 0; k < n; ++k) {
+            fail_if(idx[k] < 1 || idx[k] > m.nglob, "node index out of range");
+            o[k] = h.ref2lay[idx[k] - 1];
+        }
+        return o;
+    };
+    auto up_i = [&](DBuf<int64_t>& b, const std::vector<int64_t>& v) {
+        b.alloc(std::max<size_t>(v.size(), 1));
+        b.upload(v.data(), v.size(), s);
+    };
+    auto up_d = [&](DBuf<double>& b, const double* v, int64_t n) {
+        b.alloc(std::max<int64_t>(n, 1));
+        b.upload(v, n, s);
+    };
+    std::vector<int64_t> lBcL = to_lay(m.iBcL, m.n_iBcL), lBcT = to_lay(m.iBcT, m.n_iBcT);
+    std::vector<int64_t> lCreep = to_lay(m.FltIglobBC, m.n_FltIglobBC), lSeis = to_lay(m.out_seis, m.n_out_seis);
+    up_i(h.iBcL, lBcL);
+    up_i(h.iBcT, lBcT);
+    up_i(h.iCreep, lCreep);
+    up_i(h.iSeis, lSeis);
+    up_d(h.BcLC, m.BcLC, m.n_iBcL);
+    up_d(h.BcTC, m.BcTC, m.n_iBcT);
+    h.nBcL = (int)m.n_iBcL;
+    h.nBcT = (int)m.n_iBcT;
+    h.nCreep = (int)m.n_FltIglobBC;
+    h.nSeis = (int)m.n_out_seis;
+    fail_if(h.nSeis > 32, "at most 32 receivers");
+    h.seis.alloc(3 * std::max(h.nSeis, 1));
+
+    // fault arrays (fault order == layout row 0)
+    FaultDev& F = h.F;
+    F.Nf = Nf;
+    std::vector<int> creep(Nf, 0), bcflag(Nf, 0);
+    for (auto g : lCreep)
+        if (g < Nf) bcflag[g] = 1;
+    // iFBC (main.jl:185) is the creeping set; it must be a prefix of the fault order.
+    for (int k = 0; k < Nf; ++k) creep[k] = bcflag[k];
+    int nfbc = 0;
+    while (nfbc < Nf && creep[nfbc]) ++nfbc;
+    for (int k = nfbc; k < Nf; ++k) fail_if(creep[k], "creeping fault nodes must be the deepest ones");
+    F.NFBC0 = nfbc;
+    for (DBuf<double>* b : {&F.fo, &F.Vo, &F.xLf, &F.cca, &F.ccb, &F.Seff, &F.tauo, &F.XiLf, &F.FltB, &F.FltZ, &F.FltX,
+                            &F.Mf, &F.psi, &F.psi1, &F.psi2, &F.tau, &F.tau1, &F.tau2, &F.Vf, &F.Vf0, &F.Vf1, &F.Vf2,
+                            &F.FltVfree, &F.vPre})
+        b->alloc(Nf);
+    F.fo.upload(m.fo, Nf, s);
+    F.Vo.upload(m.Vo, Nf, s);
+    F.xLf.upload(m.xLf, Nf, s);
+    F.cca.upload(m.cca, Nf, s);
+    F.ccb.upload(m.ccb, Nf, s);
+    F.Seff.upload(m.Seff, Nf, s);
+    F.tauo.upload(m.tauo, Nf, s);
+    F.XiLf.upload(m.XiLf, Nf, s);
+    F.FltB.upload(m.FltB, Nf, s);
+    F.FltZ.upload(m.FltZ, Nf, s);
+    F.FltX.upload(m.FltX, Nf, s);
+    std::vector<double> Mf(Nf);
+    for (int k = 0; k < Nf; ++k) Mf[k] = m.M[m.iFlt[k] - 1];
+    F.Mf.upload(Mf.data(), Nf, s);
+    F.creep.alloc(Nf);
+    F.creep.upload(creep.data(), Nf, s);
+    h.bcflag.alloc(Nf);
+    h.bcflag.upload(bcflag.data(), Nf, s);
+    h.h_tauo.assign(m.tauo, m.tauo + Nf);
+    h.h_FltX.assign(m.FltX, m.FltX + Nf);
+
+    // control, reductions
+    h.ctrl.alloc(1);
+    EQC_CUDA(cudaMallocHost(&h.h_ctrl, sizeof(Ctrl)));
+    std::memset(h.h_ctrl, 0, sizeof(Ctrl));
+    h.red_part.alloc(4096);
+    h.red_count.alloc(64);
+    h.scal.alloc(16);
+    EQC_CUDA(cudaMallocHost(&h.h_scal, sizeof(double) * 16));
+    EQC_CUDA(cudaStreamSynchronize(s));
+    if (h.opt.precond == EQC_PC_AMG) mg_build(h);
+}
+
+static void to_layout(const Handle& h, const double* ref, std::vector<double>& lay) {
+    lay.assign(h.L.size(), 0.0);
+    for (int64_t g = 0; g < h.nglob; ++g) lay[h.ref2lay[g]] = ref[g];
+}
+static void from_layout(const Handle& h, const std::vector<double>& lay, double* ref) {
+    for (int64_t g = 0; g < h.nglob; ++g) ref[g] = lay[h.ref2lay[g]];
+}
+
+}  // namespace eqc
+
+using namespace eqc;
+
+
+template <class F>
+static eqc_status guarded(eqc_handle* H, F&& f) {
+    try {
+        f();
+        return EQC_OK;
+    } catch (const Error& e) {
+        if (H) H->h.err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        if (H) H->h.err = e.what();
+        return EQC_E_ARG;
+    }
+}
+
+extern "C" {
+
+void eqc_default_options(eqc_options* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->precision = EQC_FP64;
+    o->precond = EQC_PC_AMG;
+    o->guess = EQC_GUESS_PREVIOUS;
+    o->tol_rule = EQC_TOL_RHS;
+    o->cg_tol = 1e-8;
+    o->cg_maxit = 0;
+    o->device = 0;
+    o->use_graphs = 1;
+    o->verbose = 0;
+}
+
+static thread_local std::string g_create_err;
+
+eqc_status eqc_create(const eqc_model* model, const eqc_options* opt, eqc_handle** out) {
+    if (!model || !out) return EQC_E_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_create_err = "no CUDA device";
+        return EQC_E_NOGPU;
+    }
+    eqc_handle* H = new eqc_handle();
+    if (opt) H->h.opt = *opt;
+    else eqc_default_options(&H->h.opt);
+    eqc_status st = guarded(H, [&] { create(H->h, *model); });
+    if (st != EQC_OK) {
+        g_create_err = H->h.err;
+        delete H;
+        return st;
+    }
+    *out = H;
+    return EQC_OK;
+}
+
+eqc_status eqc_destroy(eqc_handle* H) {
+    if (!H) return EQC_E_ARG;
+    delete H;
+    return EQC_OK;
+}
+
+const char* eqc_last_error(const eqc_handle* H) { return H ? H->h.err.c_str() : g_create_err.c_str(); }
+
+eqc_status eqc_apply_K(eqc_handle* H, const double* x, double* y) {
+    if (!H || !x || !y) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        std::vector<double> xl, yl(h.L.size());
+        to_layout(h, x, xl);
+        h.tmp64a.upload(xl.data(), xl.size(), h.stream);
+        apply_K<double>(h.tmp64a.p, h.tmp64b.p, args64(h), 1.0, 0, h.stream);
+        h.tmp64b.download(yl.data(), yl.size(), h.stream);
+        EQC_CUDA(cudaStreamSynchronize(h.stream));
+        from_layout(h, yl, y);
+    });
+}
+
+eqc_status eqc_qs_solve(eqc_handle* H, const double* F_fault, double* d_inout, double tol, int32_t maxit,
+                        int32_t* iters, double* relres) {
+    if (!H || !F_fault || !d_inout) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        const int64_t N = h.L.size();
+        // keep the time-loop displacement intact
+        EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * N, cudaMemcpyDeviceToDevice, h.stream));
+        std::vector<double> dl;
+        to_layout(h, d_inout, dl);
+        for (int k = 0; k < h.F.Nf; ++k) dl[k] = F_fault[k];
+        h.d.upload(dl.data(), N, h.stream);
+        double rr = 0;
+        int it = qs_solve_device(h, tol, maxit, &rr);
+        h.d.download(dl.data(), N, h.stream);
+        EQC_CUDA(cudaMemcpyAsync(h.d.p, h.dPre.p, sizeof(double) * N, cudaMemcpyDeviceToDevice, h.stream));
+        EQC_CUDA(cudaStreamSynchronize(h.stream));
+        from_layout(h, dl, d_inout);
+        if (iters) *iters = it;
+        if (relres) *relres = rr;
+        if (it < 0) throw Error(EQC_E_CG, "CG reached maxit");
+    });
+}
+
+eqc_status eqc_slrFunc(eqc_handle* H, const double* psi, double* psi1, const double* Vf, double* Vf1,
+                       const double* tau1, double dt) {
+    if (!H || !psi || !psi1 || !Vf || !Vf1 || !tau1) return EQC_E_ARG;
+    return guarded(H, [&] { fault_slrFunc(H->h, psi, psi1, Vf, Vf1, tau1, dt); });
+}
+
+eqc_status eqc_FBC(eqc_handle* H, double* psi1, double* Vf1, double* tau1, double* psi2, double* Vf2, double* tau2,
+                   const double* psi, const double* Vf, const double* FltVfree, double dt, int64_t* fail_node) {
+    if (!H || !psi1 || !Vf1 || !tau1 || !psi2 || !Vf2 || !tau2 || !psi || !Vf || !FltVfree) return EQC_E_ARG;
+    return guarded(H, [&] {
+        int f = fault_FBC(H->h, psi1, Vf1, tau1, psi2, Vf2, tau2, psi, Vf, FltVfree, dt);
+        if (fail_node) *fail_node = f;
+        if (f) throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(f));
+    });
+}
+
+eqc_status eqc_dtevol(eqc_handle* H, double dt, double dtmin, const double* Vf, int32_t isolver, double* dt_out) {
+    if (!H || !Vf || !dt_out) return EQC_E_ARG;
+    return guarded(H, [&] { *dt_out = fault_dtevol(H->h, dt, dtmin, Vf, isolver); });
+}
+
+eqc_status eqc_init(eqc_handle* H, double V_init) {
+    if (!H || !(V_init > 0)) return EQC_E_ARG;
+    return guarded(H, [&] { init_state(H->h, V_init); });
+}
+
+eqc_status eqc_run(eqc_handle* H, int64_t max_steps, double t_end, eqc_run_stats* stats) {
+    if (!H) return EQC_E_ARG;
+    return guarded(H, [&] { run_steps(H->h, max_steps, t_end, stats); });
+}
+
+static DBuf<double>* state_buf(Handle& h, const std::string& s, bool& fault) {
+    fault = false;
+    if (s == "d") return &h.d;
+    if (s == "v") return &h.v;
+    if (s == "a") return &h.a;
+    fault = true;
+    if (s == "psi") return &h.F.psi;
+    if (s == "tau") return &h.F.tau;
+    return nullptr;
+}
+
+eqc_status eqc_get_state(eqc_handle* H, const char* name, double* out) {
+    if (!H || !name || !out) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        bool fault;
+        DBuf<double>* b = state_buf(h, name, fault);
+        if (!b) throw Error(EQC_E_ARG, std::string("unknown state ") + name);
+        if (fault) {
+            b->download(out, h.F.Nf, h.stream);
+            EQC_CUDA(cudaStreamSynchronize(h.stream));
+        } else {
+            std::vector<double> l(h.L.size());
+            b->download(l.data(), l.size(), h.stream);
+            EQC_CUDA(cudaStreamSynchronize(h.stream));
+            from_layout(h, l, out);
+        }
+    });
+}
+
+eqc_status eqc_set_state(eqc_handle* H, const char* name, const double* in) {
+    if (!H || !name || !in) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        bool fault;
+        DBuf<double>* b = state_buf(h, name, fault);
+        if (!b) throw Error(EQC_E_ARG, std::string("unknown state ") + name);
+        if (fault) {
+            b->upload(in, h.F.Nf, h.stream);
+        } else {
+            std::vector<double> l;
+            to_layout(h, in, l);
+            b->upload(l.data(), l.size(), h.stream);
+        }
+        EQC_CUDA(cudaStreamSynchronize(h.stream));
+    });
+}
+
+eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
+    if (!H || !name || !out) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        const std::string s(name);
+        const Ctrl& C = *h.h_ctrl;
+        if (s == "t") *out = C.t;
+        else if (s == "dt") *out = C.dt;
+        else if (s == "isolver") *out = C.isolver;
+        else if (s == "it") *out = (double)C.it;
+        else if (s == "cg_iters") *out = (double)h.cg_iters_total;
+        else if (s == "qs_solves") *out = (double)h.qs_solves_total;
+        else throw Error(EQC_E_ARG, "unknown scalar " + s);
+    });
+}
+
+static const std::vector<double>* result_field(Handle& h, const std::string& s) {
+    auto& r = h.res;
+    if (s == "seismic_stress") return &r.seismic_stress;
+    if (s == "seismic_slipvel") return &r.seismic_slipvel;
+    if (s == "seismic_slip") return &r.seismic_slip;
+    if (s == "is_stress") return &r.is_stress;
+    if (s == "is_slipvel") return &r.is_slipvel;
+    if (s == "is_slip") return &r.is_slip;
+    if (s == "dSeis") return &r.dSeis;
+    if (s == "vSeis") return &r.vSeis;
+    if (s == "aSeis") return &r.aSeis;
+    if (s == "tStart") return &r.tStart;
+    if (s == "tEnd") return &r.tEnd;
+    if (s == "hypo") return &r.hypo;
+    if (s == "taubefore") return &r.taubefore;
+    if (s == "tauafter") return &r.tauafter;
+    if (s == "delfafter") return &r.delfafter;
+    if (s == "time_") return &r.time_;
+    if (s == "Vfmax") return &r.Vfmax;
+    return nullptr;
+}
+
+int64_t eqc_result_size(eqc_handle* H, const char* field) {
+    if (!H || !field) return -1;
+    if (std::string(field) == "index_eq") return 0;
+    const std::vector<double>* f = result_field(H->h, field);
+    return f ? (int64_t)f->size() : -1;
+}
+
+// Receiver matrices are stored record-major on the host; the reference's dSeis is
+// [rit, nseis] column-major, so transpose on the way out.
+eqc_status eqc_get_result(eqc_handle* H, const char* field, double* out) {
+    if (!H || !field || !out) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        const std::string s(field);
+        const std::vector<double>* f = result_field(h, s);
+        if (!f) throw Error(EQC_E_ARG, "unknown result field " + s);
+        if ((s == "dSeis" || s == "vSeis" || s == "aSeis") && h.nSeis > 0) {
+            const int64_t nr = (int64_t)f->size() / h.nSeis;
+            for (int64_t r = 0; r < nr; ++r)
+                for (int k = 0; k < h.nSeis; ++k) out[r + nr * k] = (*f)[r * h.nSeis + k];
+        } else {
+            std::copy(f->begin(), f->end(), out);
+        }
+    });
+}
+
+eqc_status eqc_layout(eqc_handle* H, int64_t* nx, int64_t* ny, int64_t* ld) {
+    if (!H) return EQC_E_ARG;
+    if (nx) *nx = H->h.L.nx;
+    if (ny) *ny = H->h.L.ny;
+    if (ld) *ld = H->h.L.ld;
+    return EQC_OK;
+}
+
+eqc_status eqc_apply_K_device(eqc_handle* H, const void* x, void* y, int32_t dtype) {
+    if (!H || !x || !y || (dtype != 0 && dtype != 1)) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        if (dtype == 0) apply_K<double>((const double*)x, (double*)y, args64(h), 1.0, 0, h.stream);
+        else apply_K<float>((const float*)x, (float*)y, args32(h), 1.0f, 0, h.stream);
+    });
+}
+
+int64_t eqc_launch_count(eqc_handle* H) { return H ? eqc::g_launches : -1; }
+
+eqc_status eqc_sync(eqc_handle* H) {
+    if (!H) return EQC_E_ARG;
+    return guarded(H, [&] { EQC_CUDA(cudaStreamSynchronize(H->h.stream)); });
+}
+
+}  // extern "C"

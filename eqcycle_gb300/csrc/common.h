@@ -1,0 +1,99 @@
+// Internal definitions of libeqc (GB300 / sm_103a implementation of the eqcycle hot path).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <stdexcept>
+#include "../../include/eqc.h"
+
+namespace eqc {
+
+// ---- errors -----------------------------------------------------------------------
+struct Error : std::runtime_error {
+    eqc_status code;
+    Error(eqc_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define EQC_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            throw ::eqc::Error(EQC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + \
+                                               " (" + __FILE__ + ":" + std::to_string(__LINE__) + ")"); \
+    } while (0)
+
+#define EQC_CHECK_LAUNCH() EQC_CUDA(cudaGetLastError())
+
+// ---- device buffer ----------------------------------------------------------------
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void alloc(size_t count) {
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw Error(EQC_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        n = count;
+        EQC_CUDA(cudaMemset(p, 0, count * sizeof(T)));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void upload(const T* h, size_t count, cudaStream_t s) {
+        if (count) EQC_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T>& h, cudaStream_t s) {
+        if (n < h.size()) alloc(h.size());
+        upload(h.data(), h.size(), s);
+    }
+    void download(T* h, size_t count, cudaStream_t s) const {
+        if (count) EQC_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    void zero(cudaStream_t s) {
+        if (n) EQC_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
+// ---- node layout ------------------------------------------------------------------
+// Lexicographic grid of GLL nodes: ix along depth (fast), iy fault-normal.  Node
+// (ix, iy) lives at iy*ld + ix.  The fault is row iy = 0 and ix grows from the bottom
+// of the fault (x = -LX) to the free surface, the same order as iFlt.
+struct Layout {
+    int NelX, NelY;
+    int nx, ny;   // 4*NelX+1, 4*NelY+1
+    int ld;       // row pitch in elements
+    __host__ __device__ int64_t size() const { return (int64_t)ld * ny; }
+    __host__ __device__ int64_t interior_begin() const { return ld; }   // first entry of row 1
+};
+
+// Stiffness apply parameters (element data in the reference's [i,j,e] layout,
+// element e = ey*NelX + ex, src/MaterialProperties.jl:9).
+template <class T>
+struct ApplyArgs {
+    const T* W;       // [25*Nel]
+    T c1, c2;         // coefint1, coefint2 (par.jl:35-36)
+    Layout L;
+};
+
+// Kernel counters (what the library launched).
+extern int64_t g_launches;
+inline void count_launch(int n = 1) { g_launches += n; }
+
+}  // namespace eqc

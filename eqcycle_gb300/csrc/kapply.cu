@@ -1,0 +1,183 @@
+// K1: matrix-free spectral-element stiffness apply  y = sign * K x.
+//
+// Replaces the assembled SpMV Ksparse*x of src/main.jl:246,267,311 with the element
+// form of src/PCG.jl:82 (element_computation!):
+//     a_e = c1 * H * (W_e .* (H' u_e)) + c2 * (W_e .* (u_e H)) * H'
+// scattered through the connectivity (the Conn product of src/PCG.jl:266).
+//
+// GB300 design.  The mesh is structured, so node indices are computed, not loaded.
+// One CTA owns a tile of TEX x TEY elements' worth of nodes and gathers, for each
+// owned node, the contributions of the <= 4 elements containing it in a fixed order
+// (deterministic, no atomics, bitwise reproducible).  The owned node range of a tile
+// is [4*ex0, 4*(ex0+TEX)) x [4*ey0, 4*(ey0+TEY)); the elements just left of and below
+// the tile are recomputed as a halo.  Per element the work is split into 5 x-lines
+// and 5 y-lines (sum factorisation: two 5x5 contractions per line) staged through
+// shared memory.
+#include "common.h"
+
+namespace eqc {
+
+__constant__ double cH64[25];  // H[i + 5*j] = h'_i(x_j)
+__constant__ float cH32[25];
+
+template <class T> __device__ __forceinline__ T Hc(int i, int j);
+template <> __device__ __forceinline__ double Hc<double>(int i, int j) { return cH64[i + 5 * j]; }
+template <> __device__ __forceinline__ float Hc<float>(int i, int j) { return cH32[i + 5 * j]; }
+
+void set_H(const double* H, cudaStream_t s) {
+    float hf[25];
+    for (int k = 0; k < 25; ++k) hf[k] = (float)H[k];
+    EQC_CUDA(cudaMemcpyToSymbolAsync(cH64, H, sizeof(double) * 25, 0, cudaMemcpyHostToDevice, s));
+    EQC_CUDA(cudaMemcpyToSymbolAsync(cH32, hf, sizeof(float) * 25, 0, cudaMemcpyHostToDevice, s));
+    EQC_CUDA(cudaStreamSynchronize(s));
+}
+
+// mode 0: full apply, every owned node written
+// mode 1: full apply, fault row (iy = 0) written as zero (interior operator K_II)
+// mode 2: fault strip: only element row 0, x rows > 0 read as zero, rows 1..4 written
+//         (y_I = K_IF x_F, the right-hand side of the quasi-static solve)
+// mode 3: fault strip: only element row 0, row 0 written (fault traction (K d)[iFlt])
+template <class T, int TEX, int TEY>
+__global__ void __launch_bounds__(256) k_apply(const T* __restrict__ x, T* __restrict__ y, ApplyArgs<T> A,
+                                               T sign, int mode) {
+    const Layout L = A.L;
+    const bool strip = mode >= 2;
+    const int ex0 = blockIdx.x * TEX;
+    const int ey0 = strip ? 0 : blockIdx.y * TEY;
+    const int exs = max(ex0 - 1, 0), exe = min(ex0 + TEX, L.NelX);
+    const int eys = strip ? 0 : max(ey0 - 1, 0);
+    const int eye = strip ? 1 : min(ey0 + TEY, L.NelY);
+    const int nex = exe - exs, ney = eye - eys, nE = nex * ney;
+    const int tnx = 4 * nex + 1, tny = 4 * ney + 1;
+    const int ix0 = 4 * exs, iy0 = 4 * eys;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* us = reinterpret_cast<T*>(smem_raw);
+    constexpr int USZ = (4 * (TEX + 1) + 1) * (4 * (TEY + 1) + 1);
+    constexpr int ESZ = (TEX + 1) * (TEY + 1) * 25;
+    T* Ws = us + USZ;
+    T* yl = Ws + ESZ;
+
+    for (int k = threadIdx.x; k < tnx * tny; k += blockDim.x) {
+        const int a = k % tnx, b = k / tnx;
+        T v = x[(int64_t)(iy0 + b) * L.ld + ix0 + a];
+        if (mode == 2 && (iy0 + b) > 0) v = T(0);
+        us[k] = v;
+    }
+    for (int k = threadIdx.x; k < nE * 25; k += blockDim.x) {
+        const int le = k / 25, q = k - 25 * le;
+        const int lex = le % nex, ley = le / nex;
+        Ws[k] = A.W[((int64_t)(eys + ley) * L.NelX + exs + lex) * 25 + q];
+    }
+    __syncthreads();
+
+    // x-lines: for element le and GLL row j, contract along xi.
+    for (int t = threadIdx.x; t < nE * 5; t += blockDim.x) {
+        const int le = t / 5, j = t - 5 * le;
+        const int lex = le % nex, ley = le / nex;
+        const T* ul = us + (4 * ley + j) * tnx + 4 * lex;
+        const T* w = Ws + le * 25;
+        T u[5], s[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) u[k] = ul[k];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc += Hc<T>(k, p) * u[k];
+            s[p] = w[p + 5 * j] * acc;
+        }
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            T acc = T(0);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += Hc<T>(i, p) * s[p];
+            yl[le * 25 + i + 5 * j] = A.c1 * acc;
+        }
+    }
+    __syncthreads();
+    // y-lines: for element le and GLL column i, contract along eta.
+    for (int t = threadIdx.x; t < nE * 5; t += blockDim.x) {
+        const int le = t / 5, i = t - 5 * le;
+        const int lex = le % nex, ley = le / nex;
+        const T* ul = us + (4 * ley) * tnx + 4 * lex + i;
+        const T* w = Ws + le * 25;
+        T u[5], s[5];
+#pragma unroll
+        for (int l = 0; l < 5; ++l) u[l] = ul[l * tnx];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            T acc = T(0);
+#pragma unroll
+            for (int l = 0; l < 5; ++l) acc += u[l] * Hc<T>(l, p);
+            s[p] = w[i + 5 * p] * acc;
+        }
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            T acc = T(0);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += s[p] * Hc<T>(j, p);
+            yl[le * 25 + i + 5 * j] += A.c2 * acc;
+        }
+    }
+    __syncthreads();
+
+    // Gather for owned nodes.
+    const int ixb = 4 * ex0;
+    const int ixe = (ex0 + TEX >= L.NelX) ? L.nx : 4 * (ex0 + TEX);
+    int iyb, iye;
+    if (mode == 2) { iyb = 1; iye = 5; }
+    else if (mode == 3) { iyb = 0; iye = 1; }
+    else { iyb = 4 * ey0; iye = (ey0 + TEY >= L.NelY) ? L.ny : 4 * (ey0 + TEY); }
+    const int ownx = ixe - ixb, nown = ownx * (iye - iyb);
+    for (int k = threadIdx.x; k < nown; k += blockDim.x) {
+        const int ix = ixb + k % ownx, iy = iyb + k / ownx;
+        int exA, iA, exB = -1, iB = 0;
+        if (ix == 0) { exA = 0; iA = 0; }
+        else if (ix == L.nx - 1) { exA = L.NelX - 1; iA = 4; }
+        else if ((ix & 3) == 0) { exA = (ix >> 2) - 1; iA = 4; exB = ix >> 2; iB = 0; }
+        else { exA = ix >> 2; iA = ix & 3; }
+        int eyA, jA, eyB = -1, jB = 0;
+        if (iy == 0) { eyA = 0; jA = 0; }
+        else if (iy == L.ny - 1) { eyA = L.NelY - 1; jA = 4; }
+        else if ((iy & 3) == 0) { eyA = (iy >> 2) - 1; jA = 4; eyB = iy >> 2; jB = 0; }
+        else { eyA = iy >> 2; jA = iy & 3; }
+        if (strip && eyB >= 1) eyB = -1;   // strip modes: element row 0 only
+        T acc = T(0);
+        acc += yl[((eyA - eys) * nex + exA - exs) * 25 + iA + 5 * jA];
+        if (exB >= 0) acc += yl[((eyA - eys) * nex + exB - exs) * 25 + iB + 5 * jA];
+        if (eyB >= 0) {
+            acc += yl[((eyB - eys) * nex + exA - exs) * 25 + iA + 5 * jB];
+            if (exB >= 0) acc += yl[((eyB - eys) * nex + exB - exs) * 25 + iB + 5 * jB];
+        }
+        T out = sign * acc;
+        if (mode == 1 && iy == 0) out = T(0);
+        y[(int64_t)iy * L.ld + ix] = out;
+    }
+}
+
+constexpr int TEX = 8, TEY = 8;
+
+template <class T>
+static size_t apply_smem() {
+    return sizeof(T) * ((size_t)(4 * (TEX + 1) + 1) * (4 * (TEY + 1) + 1) + 2 * (size_t)(TEX + 1) * (TEY + 1) * 25);
+}
+
+template <class T>
+void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s) {
+    static bool attr_set = false;
+    const size_t sm = apply_smem<T>();
+    if (!attr_set) {
+        EQC_CUDA(cudaFuncSetAttribute(k_apply<T, TEX, TEY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr_set = true;
+    }
+    dim3 grid((A.L.NelX + TEX - 1) / TEX, mode >= 2 ? 1 : (A.L.NelY + TEY - 1) / TEY);
+    k_apply<T, TEX, TEY><<<grid, 256, sm, s>>>(x, y, A, sign, mode);
+    EQC_CHECK_LAUNCH();
+    count_launch();
+}
+
+template void apply_K<double>(const double*, double*, const ApplyArgs<double>&, double, int, cudaStream_t);
+template void apply_K<float>(const float*, float*, const ApplyArgs<float>&, float, int, cudaStream_t);
+
+}  // namespace eqc

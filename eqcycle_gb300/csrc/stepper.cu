@@ -1,0 +1,620 @@
+// The time loop of src/main.jl:220-452 on the device.
+//
+// Node arrays live in the lexicographic layout (fault = row 0, so fault node k of iFlt is
+// layout index k).  The quasi-static branch (main.jl:226-295) runs two predictor-corrector
+// passes, each one CG solve (solver.cu) plus fault-row kernels; the dynamic branch
+// (main.jl:297-345) is an explicit Newmark step with the friction Newton solve per fault
+// node (K5).  After each step a single-CTA control kernel reduces the fault slip rate
+// (Vfmax, main.jl:348), switches regime (main.jl:439-443) and computes the next dt
+// (dtevol!, src/dtevol.jl:5-44).  Output triggers (main.jl:361-436) are evaluated on the
+// host from the control block.
+#include "model.h"
+#include "fault.cuh"
+#include "reduce.cuh"
+#include <cmath>
+#include <algorithm>
+#include <chrono>
+
+namespace eqc {
+
+constexpr int FT = 1024;  // threads of the fault-row CTA
+
+// ---------------------------------------------------------------- quasi-static kernels
+// Vf0 = 2 v[iFlt] + Vpl ; Vf = Vf0 ; d[iFlt] = F = dPre[iFlt] + v[iFlt] dt  (main.jl:231-238)
+__global__ void k_qs_begin(double* __restrict__ d, const double* __restrict__ dPre, const double* __restrict__ v,
+                           double* Vf0, double* Vf, int Nf, const Ctrl* C) {
+    const double dt = C->dt, Vpl = C->Vpl;
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < Nf; k += blockDim.x * gridDim.x) {
+        const double a = 2 * v[k] + Vpl;
+        Vf0[k] = a;
+        Vf[k] = a;
+        d[k] = dPre[k] + v[k] * dt;
+    }
+}
+
+// After a pass's solve (main.jl:265-279): tau1 = -(K d)[iFlt]/FltB with a[FltIglobBC] = 0,
+// slrFunc!, Vf1[iFBC] = Vpl, Vf = (Vf0+Vf1)/2, v[iFlt] = (Vf - Vpl)/2.  If next_F, also
+// writes the next pass's F into d[iFlt].
+struct FaultArgs {
+    const double *fo, *Vo, *xLf, *cca, *ccb, *Seff, *tauo, *XiLf, *FltB, *FltZ, *Mf;
+    double *psi, *psi1, *psi2, *tau, *tau1, *tau2, *Vf, *Vf0, *Vf1, *Vf2, *FltVfree, *vPre;
+    const int* creep;     // iFBC membership
+    const int* bcflag;   // FltIglobBC membership
+    int Nf, NFBC0;
+};
+
+__global__ void k_qs_fault(const double* __restrict__ Kd0, double* __restrict__ v, double* __restrict__ d,
+                           const double* __restrict__ dPre, FaultArgs f, const Ctrl* C, int next_F) {
+    const double dt = C->dt, Vpl = C->Vpl;
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
+        const double ak = f.bcflag[k] ? 0. : Kd0[k];
+        const double t1 = -ak / f.FltB[k];
+        f.tau1[k] = t1;
+        if (k >= f.NFBC0) {
+            const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, f.Vf[k], 1e-6);
+            f.psi1[k] = p1;
+            f.Vf1[k] = dev_slr_V(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], f.tauo[k], t1, p1);
+        }
+        if (f.creep[k]) f.Vf1[k] = Vpl;
+        const double vf = (f.Vf0[k] + f.Vf1[k]) / 2;
+        f.Vf[k] = vf;
+        const double vk = 0.5 * (vf - Vpl);
+        v[k] = vk;
+        if (next_F) d[k] = dPre[k] + vk * dt;
+    }
+}
+
+// End of the quasi-static step on the fault (main.jl:283-288).
+__global__ void k_qs_end_fault(double* __restrict__ v, FaultArgs f, const Ctrl* C) {
+    const double Vpl = C->Vpl;
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
+        f.psi[k] = f.psi1[k];
+        double t = f.tau1[k];
+        if (f.creep[k]) {
+            t = 0.;
+            f.Vf1[k] = Vpl;
+        }
+        f.tau[k] = t;
+        v[k] = 0.5 * (f.Vf1[k] - Vpl);
+    }
+}
+
+// v[FltNI] = (d - dPre)/dt ; a = 0  (main.jl:289-292), rows >= 1
+__global__ void k_qs_end_bulk(const double* __restrict__ d, const double* __restrict__ dPre, double* __restrict__ v,
+                              double* __restrict__ a, int64_t ld, int64_t n, const Ctrl* C) {
+    const double dt = C->dt;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i >= ld) v[i] = (d[i] - dPre[i]) / dt;
+        a[i] = 0.;
+    }
+}
+
+// x[list] = 0 for up to three arrays
+__global__ void k_zero_list(const int64_t* __restrict__ idx, int n, double* x, double* y, double* z) {
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < n; k += blockDim.x * gridDim.x) {
+        const int64_t g = idx[k];
+        if (x) x[g] = 0.;
+        if (y) y[g] = 0.;
+        if (z) z[g] = 0.;
+    }
+}
+
+// ---------------------------------------------------------------- dynamic kernels
+// vPre on the fault; d += dt v + dt^2/2 a ; v += dt/2 a   (main.jl:299-306)
+__global__ void k_dyn_predict(double* __restrict__ d, double* __restrict__ v, const double* __restrict__ a,
+                              double* __restrict__ vPre_f, int Nf, int64_t n, const Ctrl* C) {
+    const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double vi = v[i], ai = a[i];
+        if (i < Nf) vPre_f[i] = vi;
+        d[i] = d[i] + dt * vi + (hdt2)*ai;
+        v[i] = vi + hdt * ai;
+    }
+}
+
+// a[FltIglobBC] = 0 ; absorbing boundaries (main.jl:314-318), one CTA, L then T.
+__global__ void k_dyn_bc(double* __restrict__ a, const double* __restrict__ v, const int64_t* iBC, int nBC,
+                         const int64_t* iL, const double* CL, int nL, const int64_t* iT, const double* CT, int nT) {
+    for (int k = threadIdx.x; k < nBC; k += blockDim.x) a[iBC[k]] = 0.;
+    __syncthreads();
+    for (int k = threadIdx.x; k < nL; k += blockDim.x) a[iL[k]] = a[iL[k]] - CL[k] * v[iL[k]];
+    __syncthreads();
+    for (int k = threadIdx.x; k < nT; k += blockDim.x) a[iT[k]] = a[iT[k]] - CT[k] * v[iT[k]];
+}
+
+// Fault boundary condition (main.jl:321-331): FltVfree, Vf, FBC! (two NR solves per node),
+// tau = tau2 - tauo, psi = psi2, a[iFlt] -= FltB tau.
+__global__ void k_dyn_fault(double* __restrict__ a, const double* __restrict__ v, FaultArgs f, Ctrl* C) {
+    const double dt = C->dt, hdt = C->half_dt, Vpl = C->Vpl;
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
+        const double vfree = 2 * v[k] + 2 * hdt * a[k] / f.Mf[k];
+        f.FltVfree[k] = vfree;
+        const double vf = 2 * f.vPre[k] + Vpl;
+        f.Vf[k] = vf;
+        if (k >= f.NFBC0) {
+            const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, vf, 1e-5);
+            f.psi1[k] = p1;
+            double V1, T1;
+            dev_NR(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], 0.0, f.tauo[k], p1, f.FltZ[k], vfree, &V1, &T1);
+            f.Vf1[k] = V1;
+            f.tau1[k] = T1;
+            if (vf > 1e10 || isnan(vf) || isnan(T1)) atomicMin(&C->fail, k + 1);
+            const double p2 = dev_IDS2(f.xLf[k], f.Vo[k], f.psi[k], p1, dt, vf, V1);
+            f.psi2[k] = p2;
+            double V2, T2;
+            dev_NR(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], T1, f.tauo[k], p2, f.FltZ[k], vfree, &V2, &T2);
+            f.Vf2[k] = V2;
+            f.tau2[k] = T2;
+        }
+        double t = f.tau2[k] - f.tauo[k];
+        if (f.creep[k]) t = 0.;
+        f.tau[k] = t;
+        f.psi[k] = f.psi2[k];
+        a[k] = a[k] - f.FltB[k] * t;
+    }
+}
+
+// a = a / M ; v += dt/2 a   (main.jl:336-339)
+__global__ void k_dyn_correct(double* __restrict__ a, double* __restrict__ v, const double* __restrict__ M, int64_t n,
+                              const Ctrl* C) {
+    const double hdt = C->half_dt;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double ai = a[i] / M[i];
+        a[i] = ai;
+        v[i] = v[i] + hdt * ai;
+    }
+}
+
+// ---------------------------------------------------------------- control
+// Vfmax (main.jl:348), hypocentre argmax (main.jl:367), regime switch (main.jl:439-443),
+// next dt (dtevol!, src/dtevol.jl:5-44).  One CTA.
+__global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, FaultArgs f, Ctrl* C) {
+    __shared__ double smax[FT / 32];
+    __shared__ int sidx[FT / 32];
+    __shared__ double smin[FT / 32];
+    const double Vpl = C->Vpl;
+    const double dtmax = 50.0 * 24 * 60 * 60;
+    double vmax = -INFINITY, dmin = dtmax;
+    int imax = 0x7fffffff;
+    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) {
+        const double vk = v[k];
+        if (vk > vmax) { vmax = vk; imax = k; }
+        if (k >= f.NFBC0) {
+            const double sr = fabs(2 * vk + Vpl);
+            if (sr * dtmax > f.XiLf[k]) dmin = fmin(dmin, f.XiLf[k] / sr);
+        }
+    }
+    // warp reductions: max with first index, min
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_down_sync(0xffffffffu, vmax, o);
+        const int oi = __shfl_down_sync(0xffffffffu, imax, o);
+        if (ov > vmax || (ov == vmax && oi < imax)) { vmax = ov; imax = oi; }
+        dmin = fmin(dmin, __shfl_down_sync(0xffffffffu, dmin, o));
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { smax[w] = vmax; sidx[w] = imax; smin[w] = dmin; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bv = -INFINITY, bm = dtmax;
+        int bi = 0x7fffffff;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+            if (smax[q] > bv || (smax[q] == bv && sidx[q] < bi)) { bv = smax[q]; bi = sidx[q]; }
+            bm = fmin(bm, smin[q]);
+        }
+        const double Vfmax = 2 * bv + Vpl;
+        C->Vfmax = Vfmax;
+        C->vhypo = Vfmax;
+        C->ihypo = bi;
+        const int iso = C->isolver;
+        const int next = ((iso == 1 && Vfmax < 5e-3) || (iso == 2 && Vfmax < 2e-3)) ? 1 : 2;
+        C->isolver = next;
+        double dt;
+        if (next == 1) {
+            double dtnx = bm;
+            if (C->dtmin > dtnx) dtnx = C->dtmin;
+            if (dtnx > 1.2 * C->dt) dtnx = 1.2 * C->dt;
+            dt = dtnx;
+        } else {
+            dt = C->dtmin;
+        }
+        C->dt = dt;
+    }
+}
+
+// Gather d, v, a at receivers (main.jl:433-435) into out[3*ns].
+__global__ void k_gather_seis(const int64_t* idx, int ns, const double* d, const double* v, const double* a,
+                              double* out) {
+    const int k = threadIdx.x;
+    if (k < ns) {
+        out[k] = d[idx[k]];
+        out[ns + k] = v[idx[k]];
+        out[2 * ns + k] = a[idx[k]];
+    }
+}
+
+// ---------------------------------------------------------------- host side
+static FaultArgs fargs(Handle& h, const int* bcflag) {
+    FaultDev& F = h.F;
+    FaultArgs f;
+    f.fo = F.fo.p; f.Vo = F.Vo.p; f.xLf = F.xLf.p; f.cca = F.cca.p; f.ccb = F.ccb.p; f.Seff = F.Seff.p;
+    f.tauo = F.tauo.p; f.XiLf = F.XiLf.p; f.FltB = F.FltB.p; f.FltZ = F.FltZ.p; f.Mf = F.Mf.p;
+    f.psi = F.psi.p; f.psi1 = F.psi1.p; f.psi2 = F.psi2.p; f.tau = F.tau.p; f.tau1 = F.tau1.p; f.tau2 = F.tau2.p;
+    f.Vf = F.Vf.p; f.Vf0 = F.Vf0.p; f.Vf1 = F.Vf1.p; f.Vf2 = F.Vf2.p; f.FltVfree = F.FltVfree.p; f.vPre = F.vPre.p;
+    f.creep = F.creep.p;
+    f.bcflag = bcflag;
+    f.Nf = F.Nf;
+    f.NFBC0 = F.NFBC0;
+    return f;
+}
+
+static inline int vblocks(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4 * 152); }
+
+static void launch_check() { EQC_CHECK_LAUNCH(); }
+
+// --- fault-only API helpers (eqc_slrFunc / eqc_FBC / eqc_dtevol) ---------------------------
+__global__ void k_api_slr(FaultArgs f, double dt) {
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
+        if (k < f.NFBC0) continue;
+        const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, f.Vf[k], 1e-6);
+        f.psi1[k] = p1;
+        f.Vf1[k] = dev_slr_V(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], f.tauo[k], f.tau1[k], p1);
+    }
+}
+__global__ void k_api_fbc(FaultArgs f, double dt, int* fail) {
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
+        if (k < f.NFBC0) continue;
+        const double vf = f.Vf[k], vfree = f.FltVfree[k];
+        const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, vf, 1e-5);
+        f.psi1[k] = p1;
+        double V1, T1;
+        dev_NR(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], 0.0, f.tauo[k], p1, f.FltZ[k], vfree, &V1, &T1);
+        f.Vf1[k] = V1;
+        f.tau1[k] = T1;
+        if (vf > 1e10 || isnan(vf) || isnan(T1)) atomicMin(fail, k + 1);
+        const double p2 = dev_IDS2(f.xLf[k], f.Vo[k], f.psi[k], p1, dt, vf, V1);
+        f.psi2[k] = p2;
+        double V2, T2;
+        dev_NR(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], T1, f.tauo[k], p2, f.FltZ[k], vfree, &V2, &T2);
+        f.Vf2[k] = V2;
+        f.tau2[k] = T2;
+    }
+}
+
+void fault_slrFunc(Handle& h, const double* psi, double* psi1, const double* Vf, double* Vf1, const double* tau1,
+                   double dt) {
+    FaultDev& F = h.F;
+    const int Nf = F.Nf;
+    cudaStream_t s = h.stream;
+    F.psi.upload(psi, Nf, s);
+    F.Vf.upload(Vf, Nf, s);
+    F.tau1.upload(tau1, Nf, s);
+    F.psi1.upload(psi1, Nf, s);
+    F.Vf1.upload(Vf1, Nf, s);
+    k_api_slr<<<1, FT, 0, s>>>(fargs(h, h.bcflag.p), dt);
+    launch_check();
+    count_launch();
+    F.psi1.download(psi1, Nf, s);
+    F.Vf1.download(Vf1, Nf, s);
+    EQC_CUDA(cudaStreamSynchronize(s));
+}
+
+int fault_FBC(Handle& h, double* psi1, double* Vf1, double* tau1, double* psi2, double* Vf2, double* tau2,
+              const double* psi, const double* Vf, const double* FltVfree, double dt) {
+    FaultDev& F = h.F;
+    const int Nf = F.Nf;
+    cudaStream_t s = h.stream;
+    F.psi.upload(psi, Nf, s);
+    F.Vf.upload(Vf, Nf, s);
+    F.FltVfree.upload(FltVfree, Nf, s);
+    F.psi1.upload(psi1, Nf, s);
+    F.Vf1.upload(Vf1, Nf, s);
+    F.tau1.upload(tau1, Nf, s);
+    F.psi2.upload(psi2, Nf, s);
+    F.Vf2.upload(Vf2, Nf, s);
+    F.tau2.upload(tau2, Nf, s);
+    int big = 0x7fffffff;
+    EQC_CUDA(cudaMemcpyAsync(&h.ctrl.p->fail, &big, sizeof(int), cudaMemcpyHostToDevice, s));
+    k_api_fbc<<<1, FT, 0, s>>>(fargs(h, h.bcflag.p), dt, &h.ctrl.p->fail);
+    launch_check();
+    count_launch();
+    F.psi1.download(psi1, Nf, s);
+    F.Vf1.download(Vf1, Nf, s);
+    F.tau1.download(tau1, Nf, s);
+    F.psi2.download(psi2, Nf, s);
+    F.Vf2.download(Vf2, Nf, s);
+    F.tau2.download(tau2, Nf, s);
+    int fail = 0;
+    EQC_CUDA(cudaMemcpyAsync(&fail, &h.ctrl.p->fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+    EQC_CUDA(cudaStreamSynchronize(s));
+    return fail == 0x7fffffff ? 0 : fail;
+}
+
+__global__ void k_api_dtevol(const double* Vf, FaultArgs f, double dt, double dtmin, int isolver, double* out) {
+    __shared__ double smin[FT / 32];
+    const double dtmax = 50.0 * 24 * 60 * 60;
+    double dmin = dtmax;
+    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) {
+        if (k < f.NFBC0) continue;
+        const double sr = fabs(Vf[k]);
+        if (sr * dtmax > f.XiLf[k]) dmin = fmin(dmin, f.XiLf[k] / sr);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_down_sync(0xffffffffu, dmin, o));
+    if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = dmin;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bm = dtmax;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) bm = fmin(bm, smin[q]);
+        double r;
+        if (isolver == 1) {
+            double dtnx = bm;
+            if (dtmin > dtnx) dtnx = dtmin;
+            if (dtnx > 1.2 * dt) dtnx = 1.2 * dt;
+            r = dtnx;
+        } else {
+            r = dtmin;
+        }
+        *out = r;
+    }
+}
+
+double fault_dtevol(Handle& h, double dt, double dtmin, const double* Vf, int isolver) {
+    FaultDev& F = h.F;
+    cudaStream_t s = h.stream;
+    F.Vf2.upload(Vf, F.Nf, s);
+    k_api_dtevol<<<1, FT, 0, s>>>(F.Vf2.p, fargs(h, h.bcflag.p), dt, dtmin, isolver, h.scal.p + 15);
+    launch_check();
+    count_launch();
+    double r = 0;
+    EQC_CUDA(cudaMemcpyAsync(&r, h.scal.p + 15, sizeof(double), cudaMemcpyDeviceToHost, s));
+    EQC_CUDA(cudaStreamSynchronize(s));
+    return r;
+}
+
+// --- state initialisation (main.jl:89-190) -----------------------------------------------
+__global__ void k_init_psi(const double* v, FaultArgs f) {
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x)
+        f.psi[k] = f.tauo[k] / (f.Seff[k] * f.ccb[k]) - f.fo[k] / f.ccb[k] -
+                   (f.cca[k] / f.ccb[k]) * log(2 * v[k] / f.Vo[k]);
+}
+__global__ void k_fill(double* x, double val, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = val;
+}
+// Fill value only on real nodes (row padding stays zero).
+__global__ void k_fill_nodes(double* x, double val, Layout L) {
+    const int64_t n = L.size();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = ((i % L.ld) < L.nx) ? val : 0.0;
+}
+__global__ void k_init_Vf(const double* v, FaultArgs f) {
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x)
+        f.Vf[k] = f.creep[k] ? 0. : 2 * v[k];
+}
+
+void init_state(Handle& h, double V_init) {
+    cudaStream_t s = h.stream;
+    const Layout& L = h.L;
+    const int64_t n = L.size();
+        FaultArgs f = fargs(h, h.bcflag.p);
+    h.d.zero(s);
+    h.a.zero(s);
+    h.dPre.zero(s);
+    k_fill_nodes<<<vblocks(n), 256, 0, s>>>(h.v.p, 0.5 * V_init, L);
+    k_init_psi<<<1, FT, 0, s>>>(h.v.p, f);
+    // v = v - Vpl/2 (main.jl:183)
+    k_fill_nodes<<<vblocks(n), 256, 0, s>>>(h.v.p, 0.5 * V_init - 0.5 * h.Vpl, L);
+    k_init_Vf<<<1, FT, 0, s>>>(h.v.p, f);
+    if (h.nCreep) k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, nullptr, nullptr);
+    launch_check();
+    count_launch(h.nCreep ? 5 : 4);
+    for (DBuf<double>* b : {&h.F.psi1, &h.F.psi2, &h.F.tau, &h.F.tau1, &h.F.tau2, &h.F.Vf0, &h.F.Vf1, &h.F.Vf2,
+                            &h.F.FltVfree, &h.F.vPre})
+        b->zero(s);
+    Ctrl c{};
+    c.dt = h.dt0;
+    c.dtmin = h.dt0;
+    c.half_dt = 0.5 * h.dt0;
+    c.half_dt_sq = 0.5 * (h.dt0 * h.dt0);
+    c.Vpl = h.Vpl;
+    c.t = 0.;
+    c.isolver = 1;
+    c.fail = 0x7fffffff;
+    c.it = 0;
+    *h.h_ctrl = c;
+    EQC_CUDA(cudaMemcpyAsync(h.ctrl.p, h.h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, s));
+    EQC_CUDA(cudaStreamSynchronize(s));
+    // output bookkeeping (main.jl:166-181)
+    h.res = Handle::Results();
+    h.tvsx = 5 * h.yr2sec;
+    h.tvsxinc = h.tvsx;
+    h.tevneinc = 0.5;
+    h.tevneb = h.tevne = 0;
+    h.idelevne = h.ntvsx = h.nevne = h.slipstart = h.idd = h.it_s = h.it_e = h.rit = 0;
+    h.delfref.assign(h.F.Nf, 0.0);
+    h.cg_iters_total = h.qs_solves_total = 0;
+    h.initialized = true;
+}
+
+// capacities of the reference's preallocated outputs (main.jl:154-163)
+constexpr int64_t CAP_SEISMIC = 30000, CAP_IS = 4000, CAP_SEIS = 190000, CAP_EV = 400, CAP_TIME = 1900000;
+
+static void fault_columns(Handle& h, std::vector<double>& dF, std::vector<double>& vF, std::vector<double>& tauF) {
+    const int Nf = h.F.Nf;
+    dF.resize(Nf);
+    vF.resize(Nf);
+    tauF.resize(Nf);
+    EQC_CUDA(cudaMemcpyAsync(dF.data(), h.d.p, sizeof(double) * Nf, cudaMemcpyDeviceToHost, h.stream));
+    EQC_CUDA(cudaMemcpyAsync(vF.data(), h.v.p, sizeof(double) * Nf, cudaMemcpyDeviceToHost, h.stream));
+    EQC_CUDA(cudaMemcpyAsync(tauF.data(), h.F.tau.p, sizeof(double) * Nf, cudaMemcpyDeviceToHost, h.stream));
+    EQC_CUDA(cudaStreamSynchronize(h.stream));
+}
+
+void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
+    if (!h.initialized) throw Error(EQC_E_STATE, "eqc_run before eqc_init");
+    cudaStream_t s = h.stream;
+    const Layout& L = h.L;
+    const int64_t n = L.size();
+        FaultArgs f = fargs(h, h.bcflag.p);
+    const int Nf = h.F.Nf;
+    const double Vpl = h.Vpl;
+    const std::vector<double>& tauo = h.h_tauo;
+    const std::vector<double>& FltX = h.h_FltX;
+    auto t0 = std::chrono::steady_clock::now();
+    eqc_run_stats stats{};
+    const int64_t cg0 = h.cg_iters_total, qs0 = h.qs_solves_total;
+    std::vector<double> dF, vF, tauF, seis(3 * std::max(h.nSeis, 1));
+    Ctrl& C = *h.h_ctrl;
+    while (C.t < t_end && stats.steps < max_steps) {
+        // it = it + 1 ; t = t + dt (main.jl:221-222); dt of this step is C.dt
+        C.it += 1;
+        C.t = C.t + C.dt;
+        const double tnow = C.t;
+        if ((int64_t)h.res.time_.size() >= CAP_TIME) throw Error(EQC_E_CAPACITY, "time_ capacity (1900000) exceeded");
+        h.res.time_.push_back(tnow);
+        EQC_CUDA(cudaMemcpyAsync(&h.ctrl.p->t, &C.t, sizeof(double), cudaMemcpyHostToDevice, s));
+        const int iso = C.isolver;
+        if (iso == 1) {
+            EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            k_qs_begin<<<1, FT, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.F.Vf0.p, h.F.Vf.p, Nf, h.ctrl.p);
+            launch_check();
+            count_launch();
+            for (int p1 = 0; p1 < 2; ++p1) {
+                double rr = 0;
+                int it = qs_solve_device(h, h.opt.cg_tol, h.opt.cg_maxit, &rr);
+                if (it < 0) throw Error(EQC_E_CG, "CG did not converge within maxit (relres " + std::to_string(rr) + ")");
+                apply_K<double>(h.d.p, h.tmp64b.p, args64(h), 1.0, 3, s);  // (K d)[iFlt]
+                k_qs_fault<<<1, FT, 0, s>>>(h.tmp64b.p, h.v.p, h.d.p, h.dPre.p, f, h.ctrl.p, p1 == 0);
+                launch_check();
+                count_launch();
+            }
+            k_qs_end_fault<<<1, FT, 0, s>>>(h.v.p, f, h.ctrl.p);
+            k_qs_end_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.a.p, L.ld, n, h.ctrl.p);
+            count_launch(2);
+            if (h.nCreep) {
+                k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.d.p, h.v.p, nullptr);
+                count_launch();
+            }
+            launch_check();
+            stats.qs_steps++;
+        } else {
+            k_dyn_predict<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, Nf, n, h.ctrl.p);
+            count_launch();
+            apply_K<double>(h.d.p, h.a.p, args64(h), -1.0, 0, s);
+            k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p,
+                                        h.BcTC.p, h.nBcT);
+            k_dyn_fault<<<1, FT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
+            k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, h.M.p, n, h.ctrl.p);
+            count_launch(3);
+            if (h.nCreep) {
+                k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, h.a.p, nullptr);
+                count_launch();
+            }
+            launch_check();
+            stats.dyn_steps++;
+        }
+        k_control<<<1, FT, 0, s>>>(h.v.p, f, h.ctrl.p);
+        launch_check();
+        count_launch();
+        // host mirror of the control block
+        const double t_keep = C.t;
+        const long long it_keep = C.it;
+        EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+        EQC_CUDA(cudaStreamSynchronize(s));
+        C.t = t_keep;
+        C.it = it_keep;
+        if (C.fail != 0x7fffffff)
+            throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(C.fail));
+        const double Vfmax = C.Vfmax;
+        if (!std::isfinite(Vfmax)) throw Error(EQC_E_NAN, "non-finite slip rate");
+        // ---- outputs (main.jl:361-436) ----
+        bool need_cols = (Vfmax > 1.01 * h.Vthres && h.slipstart == 0) ||
+                         (Vfmax < 0.99 * h.Vthres && h.slipstart == 1) || (tnow > h.tvsx) || (Vfmax > h.Vevne);
+        if (need_cols) fault_columns(h, dF, vF, tauF);
+        auto push_col = [&](std::vector<double>& dst, int which) {
+            for (int k = 0; k < Nf; ++k) {
+                double val;
+                if (which == 0) val = 2 * dF[k] + Vpl * tnow;
+                else if (which == 1) val = 2 * vF[k] + Vpl;
+                else val = (tauF[k] + tauo[k]) / 1e6;
+                dst.push_back(val);
+            }
+        };
+        if (Vfmax > 1.01 * h.Vthres && h.slipstart == 0) {
+            if (h.it_s >= CAP_EV) throw Error(EQC_E_CAPACITY, "event capacity (400) exceeded");
+            h.it_s += 1;
+            for (int k = 0; k < Nf; ++k) h.delfref[k] = 2 * dF[k] + Vpl * tnow;
+            h.slipstart = 1;
+            h.res.tStart.push_back(tnow);
+            push_col(h.res.taubefore, 2);
+            h.res.hypo.push_back(FltX[C.ihypo]);
+        }
+        if (Vfmax < 0.99 * h.Vthres && h.slipstart == 1) {
+            h.it_e += 1;
+            for (int k = 0; k < Nf; ++k) h.res.delfafter.push_back(2 * dF[k] + Vpl * tnow - h.delfref[k]);
+            push_col(h.res.tauafter, 2);
+            h.res.tEnd.push_back(tnow);
+            h.slipstart = 0;
+        }
+        if (tnow > h.tvsx) {
+            if (h.ntvsx >= CAP_IS) throw Error(EQC_E_CAPACITY, "interseismic snapshot capacity (4000) exceeded");
+            h.ntvsx += 1;
+            h.idd += 1;
+            push_col(h.res.is_slip, 0);
+            push_col(h.res.is_slipvel, 1);
+            push_col(h.res.is_stress, 2);
+            h.tvsx = h.tvsx + h.tvsxinc;
+        }
+        if (Vfmax > h.Vevne) {
+            if (h.idelevne == 0) {
+                if (h.nevne >= CAP_SEISMIC) throw Error(EQC_E_CAPACITY, "seismic snapshot capacity exceeded");
+                h.nevne += 1;
+                h.idd += 1;
+                h.idelevne = 1;
+                h.tevneb = tnow;
+                h.tevne = h.tevneinc;
+                push_col(h.res.seismic_slip, 0);
+                push_col(h.res.seismic_slipvel, 1);
+                push_col(h.res.seismic_stress, 2);
+            }
+            if (h.idelevne == 1 && (tnow - h.tevneb) > h.tevne) {
+                if (h.nevne >= CAP_SEISMIC) throw Error(EQC_E_CAPACITY, "seismic snapshot capacity exceeded");
+                h.nevne += 1;
+                h.idd += 1;
+                push_col(h.res.seismic_slip, 0);
+                push_col(h.res.seismic_slipvel, 1);
+                push_col(h.res.seismic_stress, 2);
+                h.tevne = h.tevne + h.tevneinc;
+            }
+        } else {
+            h.idelevne = 0;
+        }
+        if (h.opt.verbose && C.it % 500 == 0) printf("Time (yr) = %1.5g\n", tnow / h.yr2sec);
+        if (C.it % 10 == 0 && h.nSeis > 0) {
+            if (h.rit >= CAP_SEIS) throw Error(EQC_E_CAPACITY, "receiver capacity (190000) exceeded");
+            h.rit += 1;
+            k_gather_seis<<<1, 32, 0, s>>>(h.iSeis.p, h.nSeis, h.d.p, h.v.p, h.a.p, h.seis.p);
+            count_launch();
+            EQC_CUDA(cudaMemcpyAsync(seis.data(), h.seis.p, sizeof(double) * 3 * h.nSeis, cudaMemcpyDeviceToHost, s));
+            EQC_CUDA(cudaStreamSynchronize(s));
+            for (int k = 0; k < h.nSeis; ++k) {
+                h.res.dSeis.push_back(seis[k]);
+                h.res.vSeis.push_back(seis[h.nSeis + k]);
+                h.res.aSeis.push_back(seis[2 * h.nSeis + k]);
+            }
+        }
+        h.res.Vfmax.push_back(Vfmax);
+        stats.steps++;
+    }
+    stats.cg_iters = h.cg_iters_total - cg0;
+    stats.qs_solves = h.qs_solves_total - qs0;
+    stats.t = C.t;
+    stats.dt = C.dt;
+    stats.isolver = C.isolver;
+    stats.events = (int32_t)h.it_s;
+    stats.wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (st) *st = stats;
+}
+
+}  // namespace eqc

@@ -1,0 +1,217 @@
+"""The reference-facing API: ``main(P)`` and the operator entry points.
+
+``main(P, ...)`` mirrors src/main.jl:67-477: it takes the setup tuple (``set_parameters``)
+and returns the ``results`` record of main.jl:479-498, computed by libeqc on the GPU.
+``Solver`` exposes the per-operator calls a caller of the hot path uses (the stiffness
+apply that replaces ``Ksparse*x``, the quasi-static solve that replaces ``cg!``,
+``slrFunc!``, ``FBC!``, ``dtevol!``) on host arrays in the reference numbering.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _lib as L
+from .params import Params
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+@dataclass
+class Results:
+    """main.jl:479-498 (``index_eq`` is never filled by the reference and stays empty)."""
+    seismic_stress: np.ndarray
+    seismic_slipvel: np.ndarray
+    seismic_slip: np.ndarray
+    index_eq: np.ndarray
+    is_stress: np.ndarray
+    is_slipvel: np.ndarray
+    is_slip: np.ndarray
+    dSeis: np.ndarray
+    vSeis: np.ndarray
+    aSeis: np.ndarray
+    tStart: np.ndarray
+    tEnd: np.ndarray
+    taubefore: np.ndarray
+    tauafter: np.ndarray
+    delfafter: np.ndarray
+    hypo: np.ndarray
+    time_: np.ndarray
+    Vfmax: np.ndarray
+
+
+_FAULT_MATS = ("seismic_stress", "seismic_slipvel", "seismic_slip", "is_stress", "is_slipvel", "is_slip",
+               "taubefore", "tauafter", "delfafter")
+_SEIS_MATS = ("dSeis", "vSeis", "aSeis")
+
+
+class Solver:
+    """One fault model resident on one GPU (an ``eqc_handle``)."""
+
+    def __init__(self, P: Params, precision: int = L.EQC_FP64, precond: int = L.EQC_PC_AMG,
+                 guess: int = L.EQC_GUESS_PREVIOUS, cg_tol: float = 1e-8, cg_maxit: int = 0,
+                 tol_rule: int = L.EQC_TOL_RHS, device: int = 0, use_graphs: int = 1, verbose: int = 0):
+        self.P = P
+        lib = L.lib()
+        fa, ia, m = P.farray, P.iarray, P.mesh
+        keep = {}
+
+        def d(name, a):
+            keep[name] = _c(a, np.float64)
+            return L.dptr(keep[name])
+
+        def i(name, a):
+            keep[name] = _c(a, np.int64)
+            return L.iptr(keep[name])
+
+        mod = L.EqcModel()
+        mod.Nel, mod.FltNglob, mod.yr2sec = P.int_.Nel, P.int_.FltNglob, int(P.int_.yr2sec)
+        mod.IDstate, mod.nglob, mod.Total_time = P.int_.IDstate, P.int_.nglob, float(P.int_.Total_time)
+        mod.ETA, mod.Vpl, mod.Vthres, mod.Vevne, mod.dt0 = (P.float_.ETA, P.float_.Vpl, P.float_.Vthres,
+                                                          P.float_.Vevne, P.float_.dt0)
+        mod.NelX, mod.NelY, mod.NGLL, mod.dxe, mod.dye = m.NelX, m.NelY, m.NGLL, m.dxe, m.dye
+        mod.iglob = i("iglob", np.asarray(m.iglob).reshape(-1, order="F"))
+        mod.W = d("W", np.asarray(m.W).reshape(-1, order="F"))
+        mod.H = d("H", np.asarray(m.H).reshape(-1, order="F"))
+        for name in ("fo", "Vo", "xLf", "M", "BcLC", "BcTC", "FltB", "FltZ", "FltX", "cca", "ccb", "Seff", "tauo",
+                     "XiLf"):
+            setattr(mod, name, d(name, getattr(fa, name)))
+        for name in ("iFlt", "iBcL", "iBcT", "FltIglobBC", "FltNI", "out_seis"):
+            setattr(mod, name, i(name, getattr(ia, name)))
+        mod.n_iBcL, mod.n_iBcT = len(ia.iBcL), len(ia.iBcT)
+        mod.n_FltIglobBC, mod.n_FltNI, mod.n_out_seis = len(ia.FltIglobBC), len(ia.FltNI), len(ia.out_seis)
+        self.options = L.default_options(precision=precision, precond=precond, guess=guess, cg_tol=cg_tol,
+                                         cg_maxit=cg_maxit, tol_rule=tol_rule, device=device,
+                                         use_graphs=use_graphs, verbose=verbose)
+        h = C.c_void_p()
+        L.check(lib.eqc_create(C.byref(mod), C.byref(self.options), C.byref(h)), None)
+        self.h = h
+        self.nglob = P.int_.nglob
+        self.Nf = P.int_.FltNglob
+        self.nseis = len(ia.out_seis)
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().eqc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, st):
+        L.check(st, self.h)
+
+    # -- operators (host arrays, reference numbering)
+    def apply_K(self, x: np.ndarray) -> np.ndarray:
+        x = _c(x, np.float64)
+        y = np.zeros(self.nglob)
+        self._chk(L.lib().eqc_apply_K(self.h, L.dptr(x), L.dptr(y)))
+        return y
+
+    def qs_solve(self, F_fault, d, tol: float = 1e-8, maxit: int = 0):
+        F_fault = _c(F_fault, np.float64)
+        dd = np.array(d, dtype=np.float64, copy=True)
+        it = C.c_int32(0)
+        rr = C.c_double(0)
+        self._chk(L.lib().eqc_qs_solve(self.h, L.dptr(F_fault), L.dptr(dd), tol, maxit, C.byref(it), C.byref(rr)))
+        return dd, it.value, rr.value
+
+    def slrFunc(self, psi, psi1, Vf, Vf1, tau1, dt):
+        psi1 = np.array(psi1, dtype=np.float64, copy=True)
+        Vf1 = np.array(Vf1, dtype=np.float64, copy=True)
+        self._chk(L.lib().eqc_slrFunc(self.h, L.dptr(_c(psi, np.float64)), L.dptr(psi1), L.dptr(_c(Vf, np.float64)),
+                                      L.dptr(Vf1), L.dptr(_c(tau1, np.float64)), dt))
+        return psi1, Vf1
+
+    def FBC(self, psi1, Vf1, tau1, psi2, Vf2, tau2, psi, Vf, FltVfree, dt):
+        outs = [np.array(a, dtype=np.float64, copy=True) for a in (psi1, Vf1, tau1, psi2, Vf2, tau2)]
+        fail = C.c_int64(0)
+        st = L.lib().eqc_FBC(self.h, *[L.dptr(a) for a in outs], L.dptr(_c(psi, np.float64)),
+                             L.dptr(_c(Vf, np.float64)), L.dptr(_c(FltVfree, np.float64)), dt, C.byref(fail))
+        if st == 3:
+            raise L.EqcError(st, f"NR SEARCH FAILED at fault node {fail.value}")
+        self._chk(st)
+        return tuple(outs)
+
+    def dtevol(self, dt, dtmin, Vf, isolver):
+        out = C.c_double(0)
+        self._chk(L.lib().eqc_dtevol(self.h, dt, dtmin, L.dptr(_c(Vf, np.float64)), isolver, C.byref(out)))
+        return out.value
+
+    # -- time loop
+    def init(self, V_init: float):
+        self._chk(L.lib().eqc_init(self.h, V_init))
+
+    def run(self, max_steps: int, t_end: Optional[float] = None) -> Dict[str, float]:
+        t_end = self.P.int_.Total_time if t_end is None else t_end
+        st = L.EqcRunStats()
+        self._chk(L.lib().eqc_run(self.h, int(max_steps), float(t_end), C.byref(st)))
+        return st.as_dict()
+
+    def state(self, name: str) -> np.ndarray:
+        n = self.nglob if name in ("d", "v", "a") else self.Nf
+        out = np.zeros(n)
+        self._chk(L.lib().eqc_get_state(self.h, name.encode(), L.dptr(out)))
+        return out
+
+    def set_state(self, name: str, value: np.ndarray):
+        self._chk(L.lib().eqc_set_state(self.h, name.encode(), L.dptr(_c(value, np.float64))))
+
+    def scalar(self, name: str) -> float:
+        out = C.c_double(0)
+        self._chk(L.lib().eqc_get_scalar(self.h, name.encode(), C.byref(out)))
+        return out.value
+
+    def result(self, field: str) -> np.ndarray:
+        n = L.lib().eqc_result_size(self.h, field.encode())
+        if n < 0:
+            raise KeyError(field)
+        out = np.zeros(n)
+        if n:
+            self._chk(L.lib().eqc_get_result(self.h, field.encode(), L.dptr(out)))
+        if field in _FAULT_MATS:
+            return out.reshape(self.Nf, -1, order="F") if n else np.zeros((self.Nf, 0))
+        if field in _SEIS_MATS:
+            return out.reshape(-1, self.nseis, order="F") if n else np.zeros((0, self.nseis))
+        return out
+
+    def results(self) -> Results:
+        kw = {f: self.result(f) for f in Results.__dataclass_fields__ if f != "index_eq"}
+        return Results(index_eq=np.zeros(0), **kw)
+
+    def time_apply(self, dtype: int = 0, nrep: int = 20, flush_l2: bool = True) -> float:
+        ms = C.c_double(0)
+        self._chk(L.lib().eqc_time_apply(self.h, dtype, nrep, int(flush_l2), C.byref(ms)))
+        return ms.value
+
+    def launches(self) -> int:
+        return int(L.lib().eqc_launch_count(self.h))
+
+    def layout(self):
+        nx, ny, ld = C.c_int64(), C.c_int64(), C.c_int64()
+        self._chk(L.lib().eqc_layout(self.h, C.byref(nx), C.byref(ny), C.byref(ld)))
+        return nx.value, ny.value, ld.value
+
+
+def main(P: Params, V_init: Optional[float] = None, max_steps: int = 1 << 62, **solver_kw) -> Results:
+    """src/main.jl:67-477 on the GPU: run the whole simulation and return ``results``."""
+    V_init = P.cfg.V_init if V_init is None else V_init
+    with Solver(P, **solver_kw) as s:
+        s.init(V_init)
+        s.run(max_steps)
+        return s.results()

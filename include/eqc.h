@@ -1,0 +1,186 @@
+/*
+ * eqc.h -- C ABI of libeqc.so, the GB300 (sm_103a) implementation of the
+ * eqcycle time-stepping hot path.
+ *
+ * The reference (thehalfspace/eqcycle, Julia) has no FFI: its hot path is the
+ * Julia function main(P) (src/main.jl:67-477) with P built by setParameters
+ * (par.jl:15-231).  These entry points are what a Julia `ccall` shim keeping
+ * main(P)'s signature binds (the shim is shown in INTEGRATION.md).  Every
+ * entry point takes plain pointers and sizes; host arrays use the reference's
+ * layouts (Julia column-major, node indices 1-based, reference node numbering
+ * of src/MeshBox.jl:27-88).  The library copies what it needs and never keeps
+ * a caller pointer after returning.  All functions return an eqc_status.
+ *
+ * One handle = one fault model on one GPU, driven from one host thread.
+ */
+#ifndef EQC_H
+#define EQC_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    EQC_OK = 0,
+    EQC_E_ARG = 1,       /* invalid argument or model arrays                          */
+    EQC_E_CUDA = 2,      /* CUDA runtime error (message in eqc_last_error)            */
+    EQC_E_NR = 3,        /* friction Newton failed: the reference's "NR SEARCH FAILED!"
+                            (src/NRsearch_serial.jl:19-31)                            */
+    EQC_E_CG = 4,        /* CG reached maxit without meeting its tolerance            */
+    EQC_E_NAN = 5,       /* NaN/Inf detected in the state                             */
+    EQC_E_CAPACITY = 6,  /* an output array of main.jl:154-163 would overflow         */
+    EQC_E_TIMEOUT = 7,   /* a bounded device wait gave up                              */
+    EQC_E_NOMEM = 8,     /* device allocation failed                                   */
+    EQC_E_STATE = 9,     /* call out of order (e.g. run before init)                  */
+    EQC_E_NOGPU = 10     /* no usable CUDA device                                      */
+} eqc_status;
+
+/* The model: exactly the tuple main(P) receives (par.jl:227-230), plus the
+ * element data the matrix-free stiffness apply consumes (par.jl:99-152: the
+ * mesh connectivity iglob, the GLL weights-times-rigidity W and the GLL
+ * derivative matrix H), in place of the assembled Ksparse. */
+typedef struct {
+    /* params_int (par.jl:236-249) */
+    int64_t Nel, FltNglob, yr2sec, IDstate, nglob;
+    double Total_time;
+    /* params_float (par.jl:251-266) */
+    double ETA, Vpl, Vthres, Vevne, dt0;
+    /* mesh (par.jl:17-36, 99-152) */
+    int64_t NelX, NelY, NGLL;   /* NGLL must be 5 */
+    double dxe, dye;
+    const int64_t* iglob;       /* [NGLL,NGLL,Nel] column-major, 1-based        */
+    const double* W;            /* [NGLL,NGLL,Nel] column-major                 */
+    const double* H;            /* [NGLL,NGLL] column-major, H[i,j] = h'_i(x_j) */
+    /* params_farray (par.jl:268-292) */
+    const double *fo, *Vo, *xLf;            /* [FltNglob] */
+    const double* M;                        /* [nglob]    */
+    const double *BcLC, *BcTC;              /* [n_iBcL], [n_iBcT] */
+    const double *FltB, *FltZ, *FltX, *cca, *ccb, *Seff, *tauo, *XiLf;  /* [FltNglob] */
+    /* params_iarray (par.jl:294-301), 1-based */
+    const int64_t *iFlt;                    /* [FltNglob] */
+    const int64_t *iBcL, *iBcT, *FltIglobBC, *FltNI, *out_seis;
+    int64_t n_iBcL, n_iBcT, n_FltIglobBC, n_FltNI, n_out_seis;
+} eqc_model;
+
+/* Solver choices. */
+enum { EQC_FP64 = 0,      /* plain FP64: every kernel in double precision       */
+       EQC_MIXED = 1 };   /* FP32 stiffness apply + preconditioner inside an FP64
+                             reliable-update CG; FP64 friction, state, Newmark   */
+enum { EQC_PC_AMG = 0, EQC_PC_JACOBI = 1 };
+enum { EQC_GUESS_PREVIOUS = 0,   /* dnew .= d[FltNI] (src/main.jl:241)            */
+       EQC_GUESS_LEARNED = 1 };  /* learned initial guess, previous-step fallback  */
+enum { EQC_TOL_RHS = 0,          /* stop when ||r|| <= tol*||b|| (IterativeSolvers 0.8 rule) */
+       EQC_TOL_R0 = 1 };         /* stop when ||r|| <= tol*||r0||                  */
+
+typedef struct {
+    int32_t precision;   /* EQC_FP64 / EQC_MIXED                         */
+    int32_t precond;     /* EQC_PC_AMG / EQC_PC_JACOBI                   */
+    int32_t guess;       /* EQC_GUESS_PREVIOUS / EQC_GUESS_LEARNED       */
+    int32_t tol_rule;    /* EQC_TOL_RHS / EQC_TOL_R0                     */
+    double cg_tol;       /* main.jl:256 uses 1e-6; the workloads use 1e-8 */
+    int32_t cg_maxit;    /* <= 0: size of the system (IterativeSolvers default) */
+    int32_t device;      /* CUDA device ordinal                          */
+    int32_t use_graphs;  /* capture the per-step work in CUDA graphs     */
+    int32_t verbose;     /* print "Time (yr) = ..." every 500 steps (main.jl:425-427) */
+} eqc_options;
+
+typedef struct eqc_handle eqc_handle;
+
+/* Fill *opt with the defaults (FP64, AMG, previous-step guess, tol 1e-8). */
+void eqc_default_options(eqc_options* opt);
+
+/* Uploads the model, builds the device layout and the multigrid hierarchy
+ * (src/main.jl:193-211 builds its AMG once per run as well). */
+eqc_status eqc_create(const eqc_model* model, const eqc_options* opt, eqc_handle** out);
+eqc_status eqc_destroy(eqc_handle* h);
+const char* eqc_last_error(const eqc_handle* h);
+
+/* ---- hot-path operators on host arrays (reference numbering) ---------------- */
+
+/* y = K x  (replaces Ksparse*x, src/main.jl:246,267; element form src/PCG.jl:82). */
+eqc_status eqc_apply_K(eqc_handle* h, const double* x, double* y);
+
+/* Quasi-static displacement solve (src/main.jl:241-262): with F_fault [FltNglob]
+ * the fault displacement F[iFlt], solve K[FltNI,FltNI] d = -(K F)[FltNI] by
+ * preconditioned CG from the guess d_inout[FltNI]; on return d_inout[FltNI]
+ * holds the solution and d_inout[iFlt] = F_fault.  Replaces
+ * cg!(dnew, kni, rhs; Pl = aspreconditioner(ruge_stuben(kni)), tol = tol). */
+eqc_status eqc_qs_solve(eqc_handle* h, const double* F_fault, double* d_inout,
+                        double tol, int32_t maxit, int32_t* iters, double* relres);
+
+/* slrFunc! (src/otherFunctions_serial.jl:62-83) on [FltNglob] arrays. */
+eqc_status eqc_slrFunc(eqc_handle* h, const double* psi, double* psi1, const double* Vf,
+                       double* Vf1, const double* tau1, double dt);
+
+/* FBC! (src/NRsearch_serial.jl:6-43) on [FltNglob] arrays.  *fail_node gets 0,
+ * or the 1-based node where the reference stops with "NR SEARCH FAILED!"
+ * (status EQC_E_NR). */
+eqc_status eqc_FBC(eqc_handle* h, double* psi1, double* Vf1, double* tau1, double* psi2,
+                   double* Vf2, double* tau2, const double* psi, const double* Vf,
+                   const double* FltVfree, double dt, int64_t* fail_node);
+
+/* dtevol! (src/dtevol.jl:5-44). */
+eqc_status eqc_dtevol(eqc_handle* h, double dt, double dtmin, const double* Vf,
+                      int32_t isolver, double* dt_out);
+
+/* ---- the time loop (src/main.jl:67-477) ------------------------------------- */
+
+/* Initial state of main.jl:89-190 with v = V_init/2 (main.jl:102 uses
+ * V_init = 1e-3 m/s): d = a = 0, psi from tauo (main.jl:125), t = 0. */
+eqc_status eqc_init(eqc_handle* h, double V_init);
+
+typedef struct {
+    int64_t steps;         /* steps taken by this call          */
+    int64_t qs_steps, dyn_steps;
+    int64_t cg_iters;      /* CG iterations summed over QS solves */
+    int64_t qs_solves;
+    double t;              /* simulated time reached [s]         */
+    double dt;             /* next time step [s]                 */
+    int32_t isolver;       /* regime for the next step (1 QS, 2 dynamic) */
+    int32_t events;        /* events started so far               */
+    double wall_s;         /* wall time spent in this call        */
+} eqc_run_stats;
+
+/* Advance the time loop until t >= t_end or max_steps steps were taken.  The
+ * results of main.jl:154-163 accumulate on the device between calls. */
+eqc_status eqc_run(eqc_handle* h, int64_t max_steps, double t_end, eqc_run_stats* stats);
+
+/* State on the host (reference numbering): name is one of "d", "v", "a"
+ * [nglob], "psi", "tau" [FltNglob].  eqc_set_state writes it back. */
+eqc_status eqc_get_state(eqc_handle* h, const char* name, double* out);
+eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
+/* Scalars "t", "dt", "isolver", "it". */
+eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
+
+/* Results of main.jl:479-498, trimmed as in main.jl:455-472.  eqc_result_size
+ * gives the element count of a field (fault-major matrices are FltNglob x n,
+ * receiver matrices n x nseis, both column-major); eqc_get_result copies it. */
+int64_t    eqc_result_size(eqc_handle* h, const char* field);
+eqc_status eqc_get_result(eqc_handle* h, const char* field, double* out);
+
+/* ---- device-resident entry points (benchmarks, integration with device codes) */
+
+/* Internal node layout: lexicographic grid, depth fastest, fault = row 0.
+ * eqc_layout gives nx = 4*NelX+1, ny = 4*NelY+1 and the row pitch ld (elements). */
+eqc_status eqc_layout(eqc_handle* h, int64_t* nx, int64_t* ny, int64_t* ld);
+
+/* y = K x on device buffers in the internal layout, FP64 (dtype 0) or FP32
+ * (dtype 1, W held in FP32), on the handle's stream.  Asynchronous. */
+eqc_status eqc_apply_K_device(eqc_handle* h, const void* x, void* y, int32_t dtype);
+
+/* Time nrep launches of the stiffness apply with CUDA events on the handle's
+ * stream, flushing L2 between launches when flush_l2 != 0; *ms gets the mean
+ * launch duration. */
+eqc_status eqc_time_apply(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t flush_l2, double* ms);
+
+/* Kernel launches of the library since the handle was created. */
+int64_t eqc_launch_count(eqc_handle* h);
+
+/* Block until the handle's stream is idle. */
+eqc_status eqc_sync(eqc_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EQC_H */

@@ -1,0 +1,139 @@
+"""GPU parity: libeqc (through the C ABI) against the CPU oracle on the same inputs.
+
+Tolerances (FP64 paths):
+  * stiffness apply: 1e-12 relative (max-norm), the benchmark spec's bound for K x;
+  * quasi-static solve: both sides solved to a 1e-13 relative residual, solutions agree to
+    1e-10 relative (forward error is bounded by cond(K_II) x residual);
+  * friction kernels: 1e-12 relative (CUDA vs libm exp/log differ by ulps);
+  * time loop: state after the same steps agrees to 1e-8 relative (QS) / 1e-6 (dynamic).
+"""
+import numpy as np
+import pytest
+
+from eqcycle_gb300 import (EQC_FP64, EQC_MIXED, EQC_PC_JACOBI, EQC_PC_AMG, Solver, preset, reference_config,
+                           set_parameters)
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+SMALL = preset("homog48").replace(NelX=12, NelY=16, LX=6e3, LY=8e3, creep_depth=6e3)
+CFGS = {"ref-res1": reference_config(res=1), "homog48": preset("homog48"), "dz40": preset("dz40")}
+
+
+@pytest.fixture(scope="module")
+def models(eqclib, oracle_mod):
+    out = {}
+    for k, cfg in CFGS.items():
+        P = set_parameters(cfg)
+        out[k] = (cfg, P, oracle_mod.Oracle(cfg))
+    return out
+
+
+@pytest.mark.parametrize("name", list(CFGS))
+def test_apply_K_matches_oracle(models, name):
+    cfg, P, o = models[name]
+    with Solver(P, precond=EQC_PC_JACOBI) as s:
+        x = np.random.default_rng(0).uniform(-1e-3, 1e-3, P.int_.nglob)
+        y = s.apply_K(x)
+        y_ref = o.apply_K_csr(x)
+        assert rel(y, y_ref) <= 1e-12
+        assert np.array_equal(s.apply_K(x), y)   # deterministic, bitwise
+
+
+@pytest.mark.parametrize("name", ["ref-res1", "dz40"])
+def test_qs_solve_matches_oracle(models, name):
+    cfg, P, o = models[name]
+    rng = np.random.default_rng(1)
+    F = rng.uniform(0, 1e-2, P.int_.FltNglob)
+    d0 = rng.uniform(-1e-3, 1e-3, P.int_.nglob)
+    d_ref, it_ref, rr_ref = o.qs_solve(F, d0, tol=1e-13, mode=1)
+    with Solver(P, precond=EQC_PC_JACOBI) as s:
+        d, it, rr = s.qs_solve(F, d0, tol=1e-13)
+    assert it > 0 and rr <= 1e-13
+    assert rel(d, d_ref) <= 1e-10
+    iFlt = P.iarray.iFlt - 1
+    assert np.array_equal(d[iFlt], F)
+
+
+def test_friction_kernels_match_oracle(models, oracle_mod):
+    cfg, P, o = models["homog48"]
+    Nf = P.int_.FltNglob
+    rng = np.random.default_rng(2)
+    fa = P.farray
+    psi = np.log(1e-6 * (cfg.Dc / cfg.Vpl) * rng.uniform(0.5, 2, Nf) / cfg.Dc)
+    Vf = 10 ** rng.uniform(-11, 0, Nf)
+    tau1 = fa.tauo * rng.uniform(-0.05, 0.05, Nf)
+    dt = 1e3
+    with Solver(P, precond=EQC_PC_JACOBI) as s:
+        psi1, Vf1 = s.slrFunc(psi, np.zeros(Nf), Vf, np.zeros(Nf), tau1, dt)
+        p1r, V1r = np.zeros(Nf), np.zeros(Nf)
+        import ctypes as C
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        oracle_mod.lib().orc_slrFunc(o.h, dp(psi), dp(p1r), dp(Vf), dp(V1r), dp(tau1), dt)
+        assert rel(psi1, p1r) <= 1e-12 and rel(Vf1, V1r) <= 1e-12
+        # dynamic: FBC! on a coseismic-like state
+        Vfd = 10 ** rng.uniform(-9, 0.5, Nf)
+        Vfree = Vfd * rng.uniform(0.8, 1.2, Nf)
+        dts = P.float_.dt0
+        outs = s.FBC(*[np.zeros(Nf)] * 6, psi, Vfd, Vfree, dts)
+        refs = [np.zeros(Nf) for _ in range(6)]
+        fail = oracle_mod.lib().orc_FBC(o.h, *[dp(a) for a in refs], dp(psi), dp(Vfd), dp(Vfree), dts)
+        assert fail == 0
+        for a, b in zip(outs, refs):
+            assert rel(a, b) <= 1e-11
+        # dtevol!
+        for iso in (1, 2):
+            for dtp in (1e3, 1e7):
+                r = s.dtevol(dtp, P.float_.dt0, Vf, iso)
+                assert r == oracle_mod.lib().orc_dtevol(o.h, dtp, P.float_.dt0, dp(Vf), iso)
+
+
+def _run_both(cfg, nsteps, oracle_mod, tol, **kw):
+    P = set_parameters(cfg)
+    o = oracle_mod.Oracle(cfg)
+    o.run(nsteps, qs_mode=1, qs_tol=tol)
+    with Solver(P, cg_tol=tol, **kw) as s:
+        s.init(cfg.V_init)
+        st = s.run(nsteps)
+        got = {k: s.state(k) for k in ("d", "v", "psi", "tau")}
+        res = s.results()
+    ref = {k: o.state(k) for k in ("d", "v", "psi", "tau")}
+    return P, o, st, got, ref, res
+
+
+def test_time_loop_quasi_static_matches_oracle(eqclib, oracle_mod):
+    P, o, st, got, ref, res = _run_both(SMALL, 40, oracle_mod, 1e-12, precond=EQC_PC_JACOBI)
+    assert st["steps"] == 40 and st["qs_steps"] == 40
+    for k in ("d", "v", "psi", "tau"):
+        assert rel(got[k], ref[k]) <= 1e-8, k
+    assert rel(res.time_, o.get("time_")) <= 1e-12
+    assert rel(res.Vfmax, o.get("Vfmax")) <= 1e-8
+
+
+def test_time_loop_dynamic_matches_oracle(eqclib, oracle_mod):
+    # a fast initial slip rate drives the solver into the dynamic regime after one step
+    cfg = SMALL.replace(V_init=2e-2)
+    P, o, st, got, ref, res = _run_both(cfg, 60, oracle_mod, 1e-12, precond=EQC_PC_JACOBI)
+    assert st["dyn_steps"] >= 30
+    regime = o.get("regime")
+    assert int(np.sum(regime == 2)) == st["dyn_steps"]
+    for k in ("d", "v", "psi", "tau"):
+        assert rel(got[k], ref[k]) <= 1e-6, k
+    assert rel(res.Vfmax, o.get("Vfmax")) <= 1e-6
+    assert rel(res.dSeis, o.get("dSeis")) <= 1e-6
+
+
+def test_mixed_precision_qs_solve(models, oracle_mod):
+    cfg, P, o = models["dz40"]
+    rng = np.random.default_rng(4)
+    F = rng.uniform(0, 1e-2, P.int_.FltNglob)
+    d0 = np.zeros(P.int_.nglob)
+    d_ref, _, _ = o.qs_solve(F, d0, tol=1e-13, mode=1)
+    with Solver(P, precision=EQC_MIXED, precond=EQC_PC_JACOBI) as s:
+        d, it, rr = s.qs_solve(F, d0, tol=1e-8)
+    assert it > 0 and rr <= 1e-8        # certified on the FP64 true residual
+    assert rel(d, d_ref) <= 1e-5

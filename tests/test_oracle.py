@@ -1,0 +1,92 @@
+"""The CPU oracle against the reference's own data and against mathematical invariants.
+
+The GLL table is the only reference-shipped data on this path (pinned below); the rest of
+the oracle is a restatement checked through properties the reference's formulas imply.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from eqcycle_gb300.config import preset, reference_config
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "gll_05.json")
+
+
+def test_gll_matches_reference_table(oracle_mod):
+    g = json.load(open(GOLD))
+    x, w, H = oracle_mod.gll(5)
+    assert np.max(np.abs(x - np.array(g["x"]))) <= 2.3e-16
+    assert np.max(np.abs(w - np.array(g["w"]))) <= 2.3e-16
+    # the table prints 16 significant digits
+    assert np.max(np.abs(H - np.array(g["H"]))) <= 4e-15
+
+
+@pytest.mark.parametrize("cfg", [reference_config(res=1), preset("homog48"), preset("dz40")],
+                         ids=["reference-res1", "homog48", "dz40"])
+def test_stiffness_invariants(oracle_mod, cfg):
+    o = oracle_mod.Oracle(cfg)
+    K = o.csr()
+    if cfg.NelX == 48:
+        assert K.nnz == 407809   # 48x48 mesh, NGLL 5
+    scale = abs(K).max()
+    assert abs(K - K.T).max() <= 1e-14 * scale                        # symmetric
+    assert np.abs(K @ np.ones(o.nglob)).max() <= 1e-14 * scale        # constants in the null space
+    x = np.random.default_rng(3).uniform(-1, 1, o.nglob)
+    y1, y2 = o.apply_K_csr(x), o.apply_K_elem(x)                      # Kassemble.jl vs PCG.jl:82
+    assert np.abs(y1 - y2).max() <= 1e-13 * np.abs(y1).max()
+    assert float(x @ y1) > 0                                           # positive semi-definite
+
+
+def test_element_apply_single_element_check(oracle_mod):
+    """src/dump.jl:9-66 compares the element form with Ke*u for one element (seeded here)."""
+    cfg = reference_config(res=1).replace(NelX=1, NelY=1, LX=1600.0, LY=1500.0, rec_x=[], rec_y=[])
+    o = oracle_mod.Oracle(cfg)
+    u = np.random.default_rng(7).uniform(size=o.nglob)
+    assert np.allclose(o.apply_K_csr(u), o.apply_K_elem(u), rtol=0, atol=1e-12 * np.abs(o.apply_K_csr(u)).max())
+
+
+def test_qs_solve_modes_agree(oracle_mod):
+    o = oracle_mod.Oracle(reference_config(res=1))
+    F = np.random.default_rng(1).uniform(0, 1e-3, o.Nf)
+    d0 = np.zeros(o.nglob)
+    d_amg, it_amg, rr_amg = o.qs_solve(F, d0, tol=1e-12, mode=0)
+    d_jac, it_jac, rr_jac = o.qs_solve(F, d0, tol=1e-12, mode=1)
+    assert it_amg > 0 and it_jac > 0 and rr_amg <= 1e-12 and rr_jac <= 1e-12
+    assert np.abs(d_amg - d_jac).max() <= 1e-9 * np.abs(d_jac).max()
+    # the solution satisfies K[FltNI,:] d = 0 with d[iFlt] = F
+    K = o.csr()
+    NI = o.get("FltNI") - 1
+    r = (K @ d_jac)[NI]
+    assert np.linalg.norm(r) <= 1e-11 * np.linalg.norm((K[:, o.get("iFlt") - 1] @ F)[NI])
+
+
+def test_nr_fp64_vs_binary128(oracle_mod):
+    """The reference's NRsearch! iterates in BigFloat; FP64 agrees to round-off."""
+    rng = np.random.default_rng(5)
+    worst = 0.0
+    for _ in range(400):
+        V = 10 ** rng.uniform(-12, 1)
+        psi = rng.uniform(-2, 10)
+        a, b, sig = 0.015, 0.019, 50e6
+        tauo = sig * (0.6 + b * psi + a * np.log(V / 1e-6)) * rng.uniform(0.9, 1.1)
+        FltZ = 1e7 * rng.uniform(0.5, 2)
+        Vfree = V * rng.uniform(0.5, 2)
+        r64 = oracle_mod.NR(0.6, 1e-6, a, b, sig, 0.0, tauo, psi, FltZ, Vfree)
+        r128 = oracle_mod.NR(0.6, 1e-6, a, b, sig, 0.0, tauo, psi, FltZ, Vfree, quad=True)
+        assert r64[2] == r128[2]
+        worst = max(worst, abs(r64[1] - r128[1]) / abs(r128[1]))
+    assert worst <= 1e-12
+
+
+def test_time_loop_first_steps(oracle_mod):
+    cfg = preset("homog48").replace(NelX=12, NelY=12, LX=6e3, LY=6e3, creep_depth=6e3)
+    o = oracle_mod.Oracle(cfg)
+    n = o.run(20, qs_mode=1, qs_tol=1e-10)
+    assert n == 20
+    t = o.get("time_")
+    assert np.all(np.diff(t) > 0)
+    dt = np.diff(np.concatenate([[0.0], t]))
+    assert np.all(dt[1:] <= 1.2 * dt[:-1] * (1 + 1e-12))   # dtevol: growth capped at 1.2x
+    assert np.all(np.isfinite(o.state("d"))) and np.all(np.isfinite(o.state("psi")))
