@@ -49,7 +49,10 @@ struct DBuf {
             throw Error(EQC_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         }
         n = count;
+        // cudaMemset runs on the legacy default stream, which does not order with the
+        // handle's non-blocking stream: finish it before any upload can be enqueued.
         EQC_CUDA(cudaMemset(p, 0, count * sizeof(T)));
+        EQC_CUDA(cudaDeviceSynchronize());
     }
     void release() {
         if (p) cudaFree(p);

@@ -17,11 +17,13 @@
 
 namespace eqc {
 
-constexpr int FT = 1024;  // threads of the fault-row CTA
+constexpr int FT = 1024;  // threads of the single-CTA fault-row reductions
+constexpr int FNT = 128;  // threads per CTA of the per-node fault kernels
+static inline int fblocks(int Nf) { return (Nf + FNT - 1) / FNT; }
 
 // ---------------------------------------------------------------- quasi-static kernels
 // Vf0 = 2 v[iFlt] + Vpl ; Vf = Vf0 ; d[iFlt] = F = dPre[iFlt] + v[iFlt] dt  (main.jl:231-238)
-__global__ void k_qs_begin(double* __restrict__ d, const double* __restrict__ dPre, const double* __restrict__ v,
+__global__ void __launch_bounds__(FNT) k_qs_begin(double* __restrict__ d, const double* __restrict__ dPre, const double* __restrict__ v,
                            double* Vf0, double* Vf, int Nf, const Ctrl* C) {
     const double dt = C->dt, Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < Nf; k += blockDim.x * gridDim.x) {
@@ -43,7 +45,7 @@ struct FaultArgs {
     int Nf, NFBC0;
 };
 
-__global__ void k_qs_fault(const double* __restrict__ Kd0, double* __restrict__ v, double* __restrict__ d,
+__global__ void __launch_bounds__(FNT) k_qs_fault(const double* __restrict__ Kd0, double* __restrict__ v, double* __restrict__ d,
                            const double* __restrict__ dPre, FaultArgs f, const Ctrl* C, int next_F) {
     const double dt = C->dt, Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
@@ -65,7 +67,7 @@ __global__ void k_qs_fault(const double* __restrict__ Kd0, double* __restrict__ 
 }
 
 // End of the quasi-static step on the fault (main.jl:283-288).
-__global__ void k_qs_end_fault(double* __restrict__ v, FaultArgs f, const Ctrl* C) {
+__global__ void __launch_bounds__(FNT) k_qs_end_fault(double* __restrict__ v, FaultArgs f, const Ctrl* C) {
     const double Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         f.psi[k] = f.psi1[k];
@@ -124,7 +126,7 @@ __global__ void k_dyn_bc(double* __restrict__ a, const double* __restrict__ v, c
 
 // Fault boundary condition (main.jl:321-331): FltVfree, Vf, FBC! (two NR solves per node),
 // tau = tau2 - tauo, psi = psi2, a[iFlt] -= FltB tau.
-__global__ void k_dyn_fault(double* __restrict__ a, const double* __restrict__ v, FaultArgs f, Ctrl* C) {
+__global__ void __launch_bounds__(FNT) k_dyn_fault(double* __restrict__ a, const double* __restrict__ v, FaultArgs f, Ctrl* C) {
     const double dt = C->dt, hdt = C->half_dt, Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         const double vfree = 2 * v[k] + 2 * hdt * a[k] / f.Mf[k];
@@ -253,7 +255,7 @@ static inline int vblocks(int64_t n) { return (int)std::min<int64_t>((n + 255) /
 static void launch_check() { EQC_CHECK_LAUNCH(); }
 
 // --- fault-only API helpers (eqc_slrFunc / eqc_FBC / eqc_dtevol) ---------------------------
-__global__ void k_api_slr(FaultArgs f, double dt) {
+__global__ void __launch_bounds__(FNT) k_api_slr(FaultArgs f, double dt) {
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         if (k < f.NFBC0) continue;
         const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, f.Vf[k], 1e-6);
@@ -261,7 +263,7 @@ __global__ void k_api_slr(FaultArgs f, double dt) {
         f.Vf1[k] = dev_slr_V(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], f.tauo[k], f.tau1[k], p1);
     }
 }
-__global__ void k_api_fbc(FaultArgs f, double dt, int* fail) {
+__global__ void __launch_bounds__(FNT) k_api_fbc(FaultArgs f, double dt, int* fail) {
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         if (k < f.NFBC0) continue;
         const double vf = f.Vf[k], vfree = f.FltVfree[k];
@@ -291,7 +293,7 @@ void fault_slrFunc(Handle& h, const double* psi, double* psi1, const double* Vf,
     F.tau1.upload(tau1, Nf, s);
     F.psi1.upload(psi1, Nf, s);
     F.Vf1.upload(Vf1, Nf, s);
-    k_api_slr<<<1, FT, 0, s>>>(fargs(h, h.bcflag.p), dt);
+    k_api_slr<<<fblocks(h.F.Nf), FNT, 0, s>>>(fargs(h, h.bcflag.p), dt);
     launch_check();
     count_launch();
     F.psi1.download(psi1, Nf, s);
@@ -315,7 +317,7 @@ int fault_FBC(Handle& h, double* psi1, double* Vf1, double* tau1, double* psi2, 
     F.tau2.upload(tau2, Nf, s);
     int big = 0x7fffffff;
     EQC_CUDA(cudaMemcpyAsync(&h.ctrl.p->fail, &big, sizeof(int), cudaMemcpyHostToDevice, s));
-    k_api_fbc<<<1, FT, 0, s>>>(fargs(h, h.bcflag.p), dt, &h.ctrl.p->fail);
+    k_api_fbc<<<fblocks(h.F.Nf), FNT, 0, s>>>(fargs(h, h.bcflag.p), dt, &h.ctrl.p->fail);
     launch_check();
     count_launch();
     F.psi1.download(psi1, Nf, s);
@@ -373,7 +375,7 @@ double fault_dtevol(Handle& h, double dt, double dtmin, const double* Vf, int is
 }
 
 // --- state initialisation (main.jl:89-190) -----------------------------------------------
-__global__ void k_init_psi(const double* v, FaultArgs f) {
+__global__ void __launch_bounds__(FNT) k_init_psi(const double* v, FaultArgs f) {
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x)
         f.psi[k] = f.tauo[k] / (f.Seff[k] * f.ccb[k]) - f.fo[k] / f.ccb[k] -
                    (f.cca[k] / f.ccb[k]) * log(2 * v[k] / f.Vo[k]);
@@ -388,7 +390,7 @@ __global__ void k_fill_nodes(double* x, double val, Layout L) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = ((i % L.ld) < L.nx) ? val : 0.0;
 }
-__global__ void k_init_Vf(const double* v, FaultArgs f) {
+__global__ void __launch_bounds__(FNT) k_init_Vf(const double* v, FaultArgs f) {
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x)
         f.Vf[k] = f.creep[k] ? 0. : 2 * v[k];
 }
@@ -402,10 +404,10 @@ void init_state(Handle& h, double V_init) {
     h.a.zero(s);
     h.dPre.zero(s);
     k_fill_nodes<<<vblocks(n), 256, 0, s>>>(h.v.p, 0.5 * V_init, L);
-    k_init_psi<<<1, FT, 0, s>>>(h.v.p, f);
+    k_init_psi<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.v.p, f);
     // v = v - Vpl/2 (main.jl:183)
     k_fill_nodes<<<vblocks(n), 256, 0, s>>>(h.v.p, 0.5 * V_init - 0.5 * h.Vpl, L);
-    k_init_Vf<<<1, FT, 0, s>>>(h.v.p, f);
+    k_init_Vf<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.v.p, f);
     if (h.nCreep) k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, nullptr, nullptr);
     launch_check();
     count_launch(h.nCreep ? 5 : 4);
@@ -477,7 +479,7 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
         const int iso = C.isolver;
         if (iso == 1) {
             EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-            k_qs_begin<<<1, FT, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.F.Vf0.p, h.F.Vf.p, Nf, h.ctrl.p);
+            k_qs_begin<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.F.Vf0.p, h.F.Vf.p, Nf, h.ctrl.p);
             launch_check();
             count_launch();
             for (int p1 = 0; p1 < 2; ++p1) {
@@ -485,11 +487,11 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
                 int it = qs_solve_device(h, h.opt.cg_tol, h.opt.cg_maxit, &rr);
                 if (it < 0) throw Error(EQC_E_CG, "CG did not converge within maxit (relres " + std::to_string(rr) + ")");
                 apply_K<double>(h.d.p, h.tmp64b.p, args64(h), 1.0, 3, s);  // (K d)[iFlt]
-                k_qs_fault<<<1, FT, 0, s>>>(h.tmp64b.p, h.v.p, h.d.p, h.dPre.p, f, h.ctrl.p, p1 == 0);
+                k_qs_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.tmp64b.p, h.v.p, h.d.p, h.dPre.p, f, h.ctrl.p, p1 == 0);
                 launch_check();
                 count_launch();
             }
-            k_qs_end_fault<<<1, FT, 0, s>>>(h.v.p, f, h.ctrl.p);
+            k_qs_end_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.v.p, f, h.ctrl.p);
             k_qs_end_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.a.p, L.ld, n, h.ctrl.p);
             count_launch(2);
             if (h.nCreep) {
@@ -504,7 +506,7 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
             apply_K<double>(h.d.p, h.a.p, args64(h), -1.0, 0, s);
             k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p,
                                         h.BcTC.p, h.nBcT);
-            k_dyn_fault<<<1, FT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
+            k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
             k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, h.M.p, n, h.ctrl.p);
             count_launch(3);
             if (h.nCreep) {

@@ -106,8 +106,11 @@ def _run_both(cfg, nsteps, oracle_mod, tol, **kw):
 
 
 def test_time_loop_quasi_static_matches_oracle(eqclib, oracle_mod):
-    P, o, st, got, ref, res = _run_both(SMALL, 40, oracle_mod, 1e-12, precond=EQC_PC_JACOBI)
-    assert st["steps"] == 40 and st["qs_steps"] == 40
+    # the reference's own model (par.jl defaults at res = 1): creeping section below 24 km,
+    # V = 1 mm/s initially, so the displacement field is far from round-off
+    P, o, st, got, ref, res = _run_both(reference_config(res=1), 40, oracle_mod, 1e-14, precond=EQC_PC_JACOBI)
+    assert st["steps"] == 40 and st["qs_steps"] >= 10
+    assert int(np.sum(o.get("regime") == 1)) == st["qs_steps"]
     for k in ("d", "v", "psi", "tau"):
         assert rel(got[k], ref[k]) <= 1e-8, k
     assert rel(res.time_, o.get("time_")) <= 1e-12
