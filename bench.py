@@ -1,0 +1,315 @@
+"""Benchmark of the eqcycle time-stepping hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the 480x240-element damage-zone model (1.85M GLL nodes, 961 fault nodes;
+preset ``dz480``), seeded synthetic initial state (V = Vpl, theta with 1 % seeded noise).
+A step is one time step of the simulation loop (src/main.jl:220-452).  The timed window
+is the interseismic regime: the state starts at t = 0 with dt set to the step dtevol!
+gives for steady sliding at the plate rate (about 42 days), W untimed steps follow, then
+exactly K timed steps.  value = simulated years advanced in the K steps per hour of
+device time (CUDA events on the library stream).
+
+Methods: the headline runs the mixed-precision solver (FP32 stiffness apply and multigrid
+inside an FP64 reliable-update CG, FP64 friction and state); the plain FP64 method runs the
+same window and is reported beside it.  Both stop CG at ||r|| <= 1e-8 ||b||.
+
+--impl reference times the reference's algorithm on the host cores: the CPU oracle in
+reference mode (Ruge-Stueben AMG with Gauss-Seidel V-cycle inside CG, FP64 friction), the
+restatement of the Julia code (Julia is not installed here, so `julia run.jl` itself cannot
+run).  Its steps are whole QS steps, as many as fit in a time budget.
+
+N > 1 GPUs: the single-model path does not shard (replicas only); every rank advances its
+own replica and value sums the ranks' simulated years over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+YR = 365 * 24 * 3600.0
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    dist.init_process_group(backend="gloo")
+    return rank, ws, dist
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _allreduce(dist, v, op):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def steady_dt(solver, P):
+    """The step dtevol! takes for the initial steady sliding (rate-limited by XiLf/V)."""
+    Vf = 2 * solver.state("v")[P.iarray.iFlt - 1] + P.float_.Vpl
+    return solver.dtevol(1e30, P.float_.dt0, Vf, 1)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_window(P, precision, W, K, device):
+    from eqcycle_gb300 import Solver
+    s = Solver(P, precision=precision, cg_tol=1e-8, device=device)
+    s.init(P.cfg.V_init)
+    s.set_scalar("dt", steady_dt(s, P))
+    if W:
+        s.run(W)
+    t0 = s.scalar("t")
+    l0 = s.launches()
+    st = s.run(K)
+    launches = s.launches() - l0
+    sim_years = (st["t"] - t0) / YR
+    return s, st, sim_years, launches
+
+
+def cpu_baseline_sample(P, budget_s=240.0, min_steps=1):
+    """The oracle in reference mode on the host cores: whole QS steps from the same start."""
+    from oracle import pyoracle
+    nthreads = os.cpu_count() or 1
+    pyoracle.set_threads(nthreads)
+    o = pyoracle.Oracle(P.cfg)
+    # same start as the GPU window: t = 0, dt = the steady dtevol! step
+    Vf = 2 * o.state("v")[o.get("iFlt") - 1] + P.float_.Vpl
+    import ctypes as C
+    dt_s = pyoracle.lib().orc_dtevol(o.h, 1e30, P.float_.dt0, Vf.ctypes.data_as(C.POINTER(C.c_double)), 1)
+    o.set_state("dt", dt_s)
+    t_setup = time.time()
+    o.qs_solve(np.zeros(o.Nf), np.zeros(o.nglob), tol=1e-8, mode=0, maxit=1)  # builds the AMG hierarchy
+    setup_s = time.time() - t_setup
+    steps, wall, t0 = 0, 0.0, o.scalar("t")
+    while steps < min_steps or wall < budget_s * 0.5:
+        t1 = time.time()
+        n = o.run(1, qs_mode=0, qs_tol=1e-8)
+        wall += time.time() - t1
+        steps += n
+        if n == 0 or wall > budget_s:
+            break
+    sim_years = (o.scalar("t") - t0) / YR
+    cg = o.get("cg_iters")
+    return {"value": sim_years / (wall / 3600.0), "unit": "sim-years/hr", "cores": nthreads, "kind": "port",
+            "sample": f"{steps} interseismic QS step(s) of dz480 from the seeded start (dt {dt_s:.3g} s), "
+                      f"oracle reference mode: RS-AMG + symmetric Gauss-Seidel V-cycle in CG to 1e-8, "
+                      f"{int(cg.sum())} CG iterations, {wall:.1f} s wall, AMG setup {setup_s:.1f} s excluded",
+            "steps": steps, "wall_s": wall, "sim_years": sim_years}
+
+
+def bench_ours(args):
+    from eqcycle_gb300 import set_parameters, preset, EQC_FP64, EQC_MIXED
+    rank, ws, dist = _dist()
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    P = set_parameters(preset(args.workload))
+    nglob, Nel, Nf = P.int_.nglob, P.int_.Nel, P.int_.FltNglob
+    out = {}
+    # ---- plain FP64 method on the window
+    s64, st64, sy64, _ = run_window(P, EQC_FP64, args.warmup, args.steps, device)
+    s64.close()
+    # ---- headline: mixed precision; state at the window start kept for the e2e leg
+    from eqcycle_gb300 import Solver
+    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device)
+    s.init(P.cfg.V_init)
+    s.set_scalar("dt", steady_dt(s, P))
+    if args.warmup:
+        s.run(args.warmup)
+    start = {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}
+    t_start, dt_start, iso_start = s.scalar("t"), s.scalar("dt"), s.scalar("isolver")
+    clocks = Clocks(device)
+    _barrier(dist)
+    l0 = s.launches()
+    st = s.run(args.steps)
+    _barrier(dist)
+    launches = s.launches() - l0
+    clk = clocks.stop()
+    sim_years = (st["t"] - t_start) / YR
+    dev_s = st["gpu_ms"] / 1e3
+    dev_s_max = _allreduce(dist, dev_s, _max_op())
+    tot_years = _allreduce(dist, sim_years, _sum_op())
+    value = tot_years / (dev_s_max / 3600.0)
+    # ---- e2e: the same window through the C ABI with host buffers (state in, run, state out)
+    h2d = sum(start[k].nbytes for k in start) + 3 * 8
+    t1 = time.perf_counter()
+    for k, v in start.items():
+        s.set_state(k, v)
+    s.set_scalar("t", t_start)
+    s.set_scalar("dt", dt_start)
+    s.set_scalar("isolver", iso_start)
+    st_e = s.run(args.steps)
+    end = {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}
+    e2e_s = time.perf_counter() - t1
+    d2h = sum(end[k].nbytes for k in end) + args.steps * 96
+    e2e_years = (st_e["t"] - t_start) / YR
+    e2e_s_max = _allreduce(dist, e2e_s, _max_op())
+    e2e_value = _allreduce(dist, e2e_years, _sum_op()) / (e2e_s_max / 3600.0)
+    # ---- roofline of the dominant kernel (FP32 stiffness apply, L2 flushed between launches)
+    peak, peak_kind = measured_peaks()
+    ms32 = s.time_apply(1, 50, True)
+    bytes32 = 4 * (2 * nglob + 25 * Nel)
+    ms64 = s.time_apply(0, 20, True)
+    bytes64 = 8 * (2 * nglob + 25 * Nel)
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "kapply_dz480_traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("fp32_bytes_per_launch")
+    s.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "sim-years/hr", "value": value, "unit": "sim-years/hr", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / max(st["steps"], 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic: seeded initial state of the damage-zone model (no dataset)",
+        "config": {"workload": f"{args.workload}: 480x240-element damage-zone model, 1,846,081 nodes, 961 fault "
+                               f"nodes; interseismic window after {args.warmup} warm-up steps from the steady-sliding "
+                               f"start; mixed-precision multigrid-PCG (tol 1e-8)",
+                   "nodes": nglob, "fault_nodes": Nf, "parallelism": f"replicas x{ws}",
+                   "l2": "stiffness-apply roofline timed with an L2 flush between launches"},
+        "qs_step_ms": 1e3 * dev_s / max(st["qs_steps"], 1), "cg_iters_per_solve": st["cg_iters"] / max(st["qs_solves"], 1),
+        "sim_years_in_window": sim_years,
+        "plain_fp64": {"value": sy64 / (st64["gpu_ms"] / 3.6e6), "qs_step_ms": st64["gpu_ms"] / max(st64["qs_steps"], 1),
+                       "cg_iters_per_solve": st64["cg_iters"] / max(st64["qs_solves"], 1)},
+        "e2e": {"value": e2e_value, "unit": "sim-years/hr", "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps},
+        "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": bytes32 / (ms32 * 1e-3) / 1e9 / peak, "traffic": traffic,
+                     "kernel": "k_apply<float> (FP32 stiffness apply)", "peak_kind": peak_kind,
+                     "launch_us": ms32 * 1e3, "algorithmic_bytes": bytes32},
+        "fp64_apply": {"launch_us": ms64 * 1e3, "algorithmic_bytes": bytes64,
+                       "achieved_gbs": bytes64 / (ms64 * 1e-3) / 1e9},
+        "gpu_launches": launches,
+    }
+    line["speedup_vs_plain_fp64"] = value / line["plain_fp64"]["value"] if line["plain_fp64"]["value"] else None
+    if clk:
+        line["clocks"] = clk
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(P, budget_s=args.cpu_budget)
+    print(json.dumps(line), flush=True)
+
+
+def _max_op():
+    try:
+        import torch.distributed as dist
+        return dist.ReduceOp.MAX
+    except Exception:
+        return None
+
+
+def _sum_op():
+    try:
+        import torch.distributed as dist
+        return dist.ReduceOp.SUM
+    except Exception:
+        return None
+
+
+def bench_reference(args):
+    rank, ws, dist = _dist()
+    if rank != 0:
+        return
+    from eqcycle_gb300 import set_parameters, preset
+    P = set_parameters(preset(args.workload))
+    cb = cpu_baseline_sample(P, budget_s=args.cpu_budget, min_steps=max(1, min(args.steps, 1)))
+    line = {"impl": "reference", "metric": "sim-years/hr", "value": cb["value"], "unit": "sim-years/hr",
+            "n_gpus": ws, "steps": cb["steps"], "warmup": 0, "ms_per_step": 1e3 * cb["wall_s"] / max(cb["steps"], 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded initial state of the damage-zone model (no dataset)",
+            "config": {"workload": f"{args.workload}: interseismic QS steps from the steady-sliding start, "
+                                   "reference algorithm (RS-AMG + Gauss-Seidel in CG, tol 1e-8) on the host cores"},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "sim-years/hr", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dz480")
+    ap.add_argument("--cpu-budget", type=float, default=150.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

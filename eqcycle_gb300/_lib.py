@@ -51,7 +51,7 @@ class EqcOptions(C.Structure):
 class EqcRunStats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("qs_steps", C.c_int64), ("dyn_steps", C.c_int64), ("cg_iters", C.c_int64),
                 ("qs_solves", C.c_int64), ("t", C.c_double), ("dt", C.c_double), ("isolver", C.c_int32),
-                ("events", C.c_int32), ("wall_s", C.c_double)]
+                ("events", C.c_int32), ("wall_s", C.c_double), ("gpu_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -62,7 +62,7 @@ _lib: Optional[C.CDLL] = None
 # Every symbol include/eqc.h declares (checked by the CPU test suite).
 EXPORTS = ["eqc_default_options", "eqc_create", "eqc_destroy", "eqc_last_error", "eqc_apply_K", "eqc_qs_solve",
            "eqc_slrFunc", "eqc_FBC", "eqc_dtevol", "eqc_init", "eqc_run", "eqc_get_state", "eqc_set_state",
-           "eqc_get_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
+           "eqc_get_scalar", "eqc_set_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
            "eqc_time_apply", "eqc_launch_count", "eqc_sync"]
 
 
@@ -91,6 +91,7 @@ def lib() -> C.CDLL:
     L.eqc_get_state.argtypes = [P, C.c_char_p, _dp]
     L.eqc_set_state.argtypes = [P, C.c_char_p, _dp]
     L.eqc_get_scalar.argtypes = [P, C.c_char_p, _dp]
+    L.eqc_set_scalar.argtypes = [P, C.c_char_p, D]
     L.eqc_result_size.restype = I64
     L.eqc_result_size.argtypes = [P, C.c_char_p]
     L.eqc_get_result.argtypes = [P, C.c_char_p, _dp]

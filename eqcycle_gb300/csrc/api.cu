@@ -402,6 +402,26 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
     });
 }
 
+eqc_status eqc_set_scalar(eqc_handle* H, const char* name, double value) {
+    if (!H || !name) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        if (!h.initialized) throw Error(EQC_E_STATE, "eqc_set_scalar before eqc_init");
+        const std::string s(name);
+        Ctrl& C = *h.h_ctrl;
+        if (s == "t") C.t = value;
+        else if (s == "dt") {
+            if (!(value > 0)) throw Error(EQC_E_ARG, "dt must be positive");
+            C.dt = value;
+        } else if (s == "isolver") {
+            if (value != 1 && value != 2) throw Error(EQC_E_ARG, "isolver must be 1 or 2");
+            C.isolver = (int)value;
+        } else throw Error(EQC_E_ARG, "unknown or read-only scalar " + s);
+        EQC_CUDA(cudaMemcpyAsync(h.ctrl.p, h.h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, h.stream));
+        EQC_CUDA(cudaStreamSynchronize(h.stream));
+    });
+}
+
 static const std::vector<double>* result_field(Handle& h, const std::string& s) {
     auto& r = h.res;
     if (s == "seismic_stress") return &r.seismic_stress;

@@ -1,10 +1,420 @@
-// Multigrid preconditioner (placeholder until the hierarchy is built).
-#include "model.h"
+// Multigrid V-cycle on the device (see mg.h for the hierarchy).
+#include "mg.h"
+#include "reduce.cuh"
+#include <cmath>
+#include <random>
 
 namespace eqc {
-struct MGHier {};
-void mg_build(Handle& h) { (void)h; }
-void mg_destroy(Handle& h) { delete h.mg; h.mg = nullptr; }
-void mg_apply64(Handle&, const double*, double*) { throw Error(EQC_E_STATE, "multigrid not built"); }
-void mg_apply32(Handle&, const float*, float*) { throw Error(EQC_E_STATE, "multigrid not built"); }
+
+// ------------------------------------------------------------------ device kernels
+template <class T>
+__global__ void k_stencil(const T* __restrict__ A, const T* __restrict__ x, T* __restrict__ y, int cx, int cy) {
+    const int64_t N = (int64_t)cx * cy;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % cx), iy = (int)(i / cx);
+        T s = T(0);
+        if (iy >= 1) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const int gx = ix + (k % 3) - 1, gy = iy + (k / 3) - 1;
+                if (gx >= 0 && gx < cx && gy >= 1 && gy < cy) s += A[k * N + i] * x[(int64_t)gy * cx + gx];
+            }
+        }
+        y[i] = s;
+    }
+}
+
+// xf[fine] += sum_{a,b} wx_a wy_b xc[coarse]   (fine rows >= 1)
+template <class T>
+__global__ void k_prolong_add(const T* __restrict__ xc, T* __restrict__ xf, int nfx, int nfy, int ldf, int ldc,
+                              const int* __restrict__ px, const int* __restrict__ py, const T* __restrict__ wx,
+                              const T* __restrict__ wy) {
+    const int64_t N = (int64_t)nfx * nfy;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % nfx), iy = (int)(i / nfx);
+        if (iy == 0) continue;
+        T s = T(0);
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            const T wb = wy[2 * iy + b];
+            if (wb == T(0)) continue;
+            const int cyi = py[2 * iy + b];
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const T wa = wx[2 * ix + a];
+                if (wa != T(0)) s += wa * wb * xc[(int64_t)cyi * ldc + px[2 * ix + a]];
+            }
+        }
+        xf[(int64_t)iy * ldf + ix] += s;
+    }
+}
+
+// bc[coarse] = sum over restriction lists of rf[fine]  (coarse rows >= 1; row 0 = 0)
+template <class T>
+__global__ void k_restrict(const T* __restrict__ rf, T* __restrict__ bc, int ncx, int ncy, int ldf, int ldc,
+                           const int* __restrict__ rpx, const int* __restrict__ rix, const T* __restrict__ rwx,
+                           const int* __restrict__ rpy, const int* __restrict__ riy, const T* __restrict__ rwy) {
+    const int64_t N = (int64_t)ncx * ncy;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int cxi = (int)(i % ncx), cyi = (int)(i / ncx);
+        T s = T(0);
+        if (cyi >= 1) {
+            for (int q = rpy[cyi]; q < rpy[cyi + 1]; ++q) {
+                const int fy = riy[q];
+                if (fy == 0) continue;
+                const T wq = rwy[q];
+                T sx = T(0);
+                for (int p = rpx[cxi]; p < rpx[cxi + 1]; ++p) sx += rwx[p] * rf[(int64_t)fy * ldf + rix[p]];
+                s += wq * sx;
+            }
+        }
+        bc[(int64_t)cyi * ldc + cxi] = s;
+    }
+}
+
+// Chebyshev, first step.  with_x: r = Dinv (b - t) with t = A x ; else r = Dinv b, x = 0.
+// d = r/theta ; x += d
+template <class T>
+__global__ void k_cheb_first(T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, const T* __restrict__ b,
+                             const T* __restrict__ t, const T* __restrict__ Dinv, int64_t n, T inv_theta, int with_x) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T ri = with_x ? Dinv[i] * (b[i] - t[i]) : Dinv[i] * b[i];
+        const T di = ri * inv_theta;
+        r[i] = ri;
+        d[i] = di;
+        x[i] = with_x ? x[i] + di : di;
+    }
+}
+// Chebyshev, later step: r -= Dinv t (t = A d) ; d = c1 d + c2 r ; x += d
+template <class T>
+__global__ void k_cheb_step(T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, const T* __restrict__ t,
+                            const T* __restrict__ Dinv, int64_t n, T c1, T c2) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T ri = r[i] - Dinv[i] * t[i];
+        const T di = c1 * d[i] + c2 * ri;
+        r[i] = ri;
+        d[i] = di;
+        x[i] += di;
+    }
+}
+// r = b - t
+template <class T>
+__global__ void k_sub(const T* __restrict__ b, const T* __restrict__ t, T* __restrict__ r, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = b[i] - t[i];
+}
+// x[cx + k] = sum_j Cinv[k][j] b[cx + j]  (one warp per row)
+template <class T>
+__global__ void k_dense_mv(const T* __restrict__ Cinv, const T* __restrict__ b, T* __restrict__ x, int n, int off) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) s += (double)Cinv[(int64_t)warp * n + j] * (double)b[off + j];
+    s = warp_sum(s);
+    if (lane == 0) x[off + warp] = (T)s;
+}
+template <class T>
+__global__ void k_scale(T* x, int64_t n, double s) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = (T)((double)x[i] * s);
+}
+template <class T>
+__global__ void k_mul(const T* a, T* x, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = a[i] * x[i];
+}
+
+static inline int vb(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 8 * 152); }
+
+// ------------------------------------------------------------------ typed access
+template <class T> struct Sel;
+template <> struct Sel<double> {
+    static double* x(MGWork& w) { return w.x64.p; }
+    static double* b(MGWork& w) { return w.b64.p; }
+    static double* r(MGWork& w) { return w.r64.p; }
+    static double* d(MGWork& w) { return w.d64.p; }
+    static double* t(MGWork& w) { return w.t64.p; }
+    static const double* A(StencilLevel& l) { return l.A64.p; }
+    static const double* Di(StencilLevel& l) { return l.Dinv64.p; }
+    static const double* Di0(MGHier& m) { return m.Dinv0_64.p; }
+    static const double* C(MGHier& m) { return m.Cinv64.p; }
+    static const double* wx(DevTransfer& t) { return t.wx64.p; }
+    static const double* wy(DevTransfer& t) { return t.wy64.p; }
+    static const double* rwx(DevTransfer& t) { return t.rwx64.p; }
+    static const double* rwy(DevTransfer& t) { return t.rwy64.p; }
+    static ApplyArgs<double> args(Handle& h) { return args64(h); }
+};
+template <> struct Sel<float> {
+    static float* x(MGWork& w) { return w.x32.p; }
+    static float* b(MGWork& w) { return w.b32.p; }
+    static float* r(MGWork& w) { return w.r32.p; }
+    static float* d(MGWork& w) { return w.d32.p; }
+    static float* t(MGWork& w) { return w.t32.p; }
+    static const float* A(StencilLevel& l) { return l.A32.p; }
+    static const float* Di(StencilLevel& l) { return l.Dinv32.p; }
+    static const float* Di0(MGHier& m) { return m.Dinv0_32.p; }
+    static const float* C(MGHier& m) { return m.Cinv32.p; }
+    static const float* wx(DevTransfer& t) { return t.wx32.p; }
+    static const float* wy(DevTransfer& t) { return t.wy32.p; }
+    static const float* rwx(DevTransfer& t) { return t.rwx32.p; }
+    static const float* rwy(DevTransfer& t) { return t.rwy32.p; }
+    static ApplyArgs<float> args(Handle& h) { return args32(h); }
+};
+
+// y = A_l x on level l (0 = spectral-element grid)
+template <class T>
+static void level_apply(Handle& h, int l, const T* x, T* y) {
+    MGHier& m = *h.mg;
+    if (l == 0) {
+        apply_K<T>(x, y, Sel<T>::args(h), T(1), 1, h.stream);
+    } else {
+        StencilLevel& L = m.lev[l - 1];
+        k_stencil<T><<<vb((int64_t)L.cx * L.cy), 256, 0, h.stream>>>(Sel<T>::A(L), x, y, L.cx, L.cy);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+    }
+}
+
+static int64_t level_size(Handle& h, int l) {
+    return l == 0 ? h.L.size() : (int64_t)h.mg->lev[l - 1].cx * h.mg->lev[l - 1].cy;
+}
+
+// Chebyshev smoothing of A_l x = b (deg steps), x = 0 initially when !with_x.
+template <class T>
+static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x) {
+    MGHier& m = *h.mg;
+    MGWork& w = m.work[l];
+    const int64_t n = level_size(h, l);
+    const T* Dinv = (l == 0) ? Sel<T>::Di0(m) : Sel<T>::Di(m.lev[l - 1]);
+    const double lmax = (l == 0) ? m.lmax0 : m.lev[l - 1].lmax;
+    const double lmin = lmax / m.lo_ratio;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    const double sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    T* r = Sel<T>::r(w);
+    T* d = Sel<T>::d(w);
+    T* t = Sel<T>::t(w);
+    if (with_x) level_apply<T>(h, l, x, t);
+    k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)(1.0 / theta), with_x ? 1 : 0);
+    count_launch();
+    for (int k = 1; k < m.deg; ++k) {
+        level_apply<T>(h, l, d, t);
+        const double rho_new = 1.0 / (2.0 * sigma - rho);
+        k_cheb_step<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, t, Dinv, n, (T)(rho_new * rho), (T)(2.0 * rho_new / delta));
+        count_launch();
+        rho = rho_new;
+    }
+    EQC_CHECK_LAUNCH();
+}
+
+template <class T>
+static void vcycle(Handle& h, int l, T* x, const T* b) {
+    MGHier& m = *h.mg;
+    const int L = (int)m.lev.size();
+    if (l == L) {  // coarsest: dense solve on rows >= 1
+        StencilLevel& c = m.lev[L - 1];
+        const int64_t n = (int64_t)c.cx * c.cy;
+        EQC_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * c.cx, h.stream));
+        k_dense_mv<T><<<(m.nc * 32 + 255) / 256, 256, 0, h.stream>>>(Sel<T>::C(m), b, x, m.nc, c.cx);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+        (void)n;
+        return;
+    }
+    MGWork& w = m.work[l];
+    const int64_t n = level_size(h, l);
+    chebyshev<T>(h, l, x, b, false);
+    // residual
+    T* t = Sel<T>::t(w);
+    T* r = Sel<T>::r(w);
+    level_apply<T>(h, l, x, t);
+    k_sub<T><<<vb(n), 256, 0, h.stream>>>(b, t, r, n);
+    count_launch();
+    DevTransfer& tr = m.T[l];
+    MGWork& wc = m.work[l + 1];
+    T* bc = Sel<T>::b(wc);
+    T* xc = Sel<T>::x(wc);
+    k_restrict<T><<<vb((int64_t)tr.ncx * tr.ncy), 256, 0, h.stream>>>(r, bc, tr.ncx, tr.ncy, tr.ldf, tr.ldc, tr.rpx.p,
+                                                                       tr.rix.p, Sel<T>::rwx(tr), tr.rpy.p, tr.riy.p,
+                                                                       Sel<T>::rwy(tr));
+    count_launch();
+    vcycle<T>(h, l + 1, xc, bc);
+    k_prolong_add<T><<<vb((int64_t)tr.nfx * tr.nfy), 256, 0, h.stream>>>(xc, x, tr.nfx, tr.nfy, tr.ldf, tr.ldc, tr.px.p,
+                                                                         tr.py.p, Sel<T>::wx(tr), Sel<T>::wy(tr));
+    count_launch();
+    EQC_CHECK_LAUNCH();
+    chebyshev<T>(h, l, x, b, true);
+}
+
+// z = M^{-1} r for the CG: r, z are the interior slices (rows >= 1) of level-0 vectors.
+void mg_apply64(Handle& h, const double* r, double* z) {
+    if (!h.mg) throw Error(EQC_E_STATE, "multigrid not built");
+    const int64_t ld = h.L.ld;
+    vcycle<double>(h, 0, z - ld, r - ld);
+}
+void mg_apply32(Handle& h, const float* r, float* z) {
+    if (!h.mg) throw Error(EQC_E_STATE, "multigrid not built");
+    const int64_t ld = h.L.ld;
+    vcycle<float>(h, 0, z - ld, r - ld);
+}
+
+// ------------------------------------------------------------------ setup
+static void upload_transfer(Handle& h, DevTransfer& d, const Transfer1D& tx, const Transfer1D& ty, int ldf, int ldc) {
+    cudaStream_t s = h.stream;
+    d.nfx = tx.nf;
+    d.nfy = ty.nf;
+    d.ncx = tx.nc;
+    d.ncy = ty.nc;
+    d.ldf = ldf;
+    d.ldc = ldc;
+    auto up_i = [&](DBuf<int>& b, const std::vector<int>& v) { b.alloc(v.size()); b.upload(v.data(), v.size(), s); };
+    auto up_w = [&](DBuf<double>& b64, DBuf<float>& b32, const std::vector<double>& v) {
+        b64.alloc(v.size());
+        b64.upload(v.data(), v.size(), s);
+        std::vector<float> f(v.begin(), v.end());
+        b32.alloc(f.size());
+        b32.upload(f.data(), f.size(), s);
+    };
+    up_i(d.px, tx.p_idx);
+    up_i(d.py, ty.p_idx);
+    up_w(d.wx64, d.wx32, tx.p_w);
+    up_w(d.wy64, d.wy32, ty.p_w);
+    up_i(d.rpx, tx.r_ptr);
+    up_i(d.rix, tx.r_idx);
+    up_w(d.rwx64, d.rwx32, tx.r_w);
+    up_i(d.rpy, ty.r_ptr);
+    up_i(d.riy, ty.r_idx);
+    up_w(d.rwy64, d.rwy32, ty.r_w);
+    EQC_CUDA(cudaStreamSynchronize(s));
+}
+
+static void alloc_work(MGWork& w, int64_t n) {
+    for (DBuf<double>* b : {&w.x64, &w.b64, &w.r64, &w.d64, &w.t64}) b->alloc(n);
+    for (DBuf<float>* b : {&w.x32, &w.b32, &w.r32, &w.d32, &w.t32}) b->alloc(n);
+}
+
+// Largest eigenvalue of D^-1 A_l by power iteration (FP64, 30 steps), times 1.1.
+static double estimate_lmax(Handle& h, int l) {
+    MGHier& m = *h.mg;
+    MGWork& w = m.work[l];
+    const int64_t n = level_size(h, l);
+    const double* Dinv = (l == 0) ? m.Dinv0_64.p : m.lev[l - 1].Dinv64.p;
+    std::vector<double> x0(n);
+    std::mt19937_64 rng(1234 + l);
+    std::uniform_real_distribution<double> U(0.5, 1.5);
+    const int nx = (l == 0) ? h.L.ld : m.lev[l - 1].cx;
+    for (int64_t i = 0; i < n; ++i) x0[i] = (i < nx) ? 0.0 : U(rng);
+    w.x64.upload(x0.data(), n, h.stream);
+    double lam = 0.0;
+    for (int it = 0; it < 30; ++it) {
+        level_apply<double>(h, l, w.x64.p, w.t64.p);
+        k_mul<double><<<vb(n), 256, 0, h.stream>>>(Dinv, w.t64.p, n);
+        dot64(h, w.t64.p, w.t64.p, n, h.scal.p + 14);
+        dot64(h, w.x64.p, w.t64.p, n, h.scal.p + 13);
+        dot64(h, w.x64.p, w.x64.p, n, h.scal.p + 12);
+        double sc[3];
+        EQC_CUDA(cudaMemcpyAsync(sc, h.scal.p + 12, sizeof(double) * 3, cudaMemcpyDeviceToHost, h.stream));
+        EQC_CUDA(cudaStreamSynchronize(h.stream));
+        lam = std::sqrt(sc[2] / sc[0]);
+        EQC_CUDA(cudaMemcpyAsync(w.x64.p, w.t64.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, h.stream));
+        k_scale<double><<<vb(n), 256, 0, h.stream>>>(w.x64.p, n, 1.0 / std::sqrt(sc[2]));
+        count_launch(2);
+    }
+    EQC_CHECK_LAUNCH();
+    return 1.1 * lam;
+}
+
+void mg_build(Handle& h) {
+    mg_destroy(h);
+    h.mg = new MGHier();
+    MGHier& m = *h.mg;
+    const Layout& L = h.L;
+    cudaStream_t s = h.stream;
+    static const double xg[5] = {-1.0, -0.65465367070797714, 0.0, 0.65465367070797714, 1.0};
+    // level 0 Jacobi scaling
+    {
+        std::vector<double> dg(L.size());
+        h.diag64.download(dg.data(), dg.size(), s);
+        EQC_CUDA(cudaStreamSynchronize(s));
+        std::vector<double> di(L.size(), 0.0);
+        for (int64_t i = L.ld; i < L.size(); ++i) di[i] = ((i % L.ld) < L.nx) ? 1.0 / dg[i] : 0.0;
+        std::vector<float> df(di.begin(), di.end());
+        m.Dinv0_64.alloc(L.size());
+        m.Dinv0_64.upload(di.data(), di.size(), s);
+        m.Dinv0_32.alloc(L.size());
+        m.Dinv0_32.upload(df.data(), df.size(), s);
+    }
+    // level 1: vertex grid
+    std::vector<double> Wh((size_t)25 * h.Nel);
+    h.W64.download(Wh.data(), Wh.size(), s);
+    EQC_CUDA(cudaStreamSynchronize(s));
+    std::vector<Transfer1D> tx, ty;
+    tx.push_back(make_gll_transfer(L.NelX, xg));
+    ty.push_back(make_gll_transfer(L.NelY, xg));
+    StencilLevel l1;
+    l1.cx = L.NelX + 1;
+    l1.cy = L.NelY + 1;
+    l1.A = vertex_operator(h, Wh.data());
+    m.lev.push_back(std::move(l1));
+    // coarser vertex grids
+    while ((int64_t)m.lev.back().cx * (m.lev.back().cy - 1) > 1024 && m.lev.back().cx >= 5 && m.lev.back().cy >= 5) {
+        StencilLevel& f = m.lev.back();
+        Transfer1D ax = make_coarsen_transfer(f.cx), ay = make_coarsen_transfer(f.cy);
+        StencilLevel c;
+        c.cx = ax.nc;
+        c.cy = ay.nc;
+        c.A = galerkin_stencil(f.A, f.cx, f.cy, ax, ay, c.cx, c.cy);
+        tx.push_back(std::move(ax));
+        ty.push_back(std::move(ay));
+        m.lev.push_back(std::move(c));
+    }
+    // upload stencils and diagonal scalings
+    for (StencilLevel& lv : m.lev) {
+        const size_t N = (size_t)lv.cx * lv.cy;
+        std::vector<float> a32(lv.A.begin(), lv.A.end());
+        lv.A64.alloc(9 * N);
+        lv.A64.upload(lv.A.data(), 9 * N, s);
+        lv.A32.alloc(9 * N);
+        lv.A32.upload(a32.data(), 9 * N, s);
+        std::vector<double> di(N, 0.0);
+        for (size_t i = lv.cx; i < N; ++i) di[i] = 1.0 / lv.A[4 * N + i];
+        std::vector<float> df(di.begin(), di.end());
+        lv.Dinv64.alloc(N);
+        lv.Dinv64.upload(di.data(), N, s);
+        lv.Dinv32.alloc(N);
+        lv.Dinv32.upload(df.data(), N, s);
+        EQC_CUDA(cudaStreamSynchronize(s));
+    }
+    // transfers: T[0] SEM -> vertex grid, T[k] lev[k-1] -> lev[k]
+    m.T.resize(m.lev.size());
+    upload_transfer(h, m.T[0], tx[0], ty[0], L.ld, m.lev[0].cx);
+    for (size_t k = 1; k < m.lev.size(); ++k)
+        upload_transfer(h, m.T[k], tx[k], ty[k], m.lev[k - 1].cx, m.lev[k].cx);
+    // coarsest dense inverse
+    {
+        StencilLevel& c = m.lev.back();
+        std::vector<double> inv = dense_inverse_spd(c.A, c.cx, c.cy, m.nc);
+        std::vector<float> f(inv.begin(), inv.end());
+        m.Cinv64.alloc(inv.size());
+        m.Cinv64.upload(inv.data(), inv.size(), s);
+        m.Cinv32.alloc(f.size());
+        m.Cinv32.upload(f.data(), f.size(), s);
+    }
+    // work vectors
+    m.work.resize(m.lev.size() + 1);
+    alloc_work(m.work[0], L.size());
+    for (size_t k = 0; k < m.lev.size(); ++k) alloc_work(m.work[k + 1], (int64_t)m.lev[k].cx * m.lev[k].cy);
+    EQC_CUDA(cudaStreamSynchronize(s));
+    // spectral bounds for Chebyshev (all levels but the coarsest, which is solved directly)
+    m.lmax0 = estimate_lmax(h, 0);
+    for (size_t k = 0; k + 1 < m.lev.size(); ++k) m.lev[k].lmax = estimate_lmax(h, (int)k + 1);
+    EQC_CUDA(cudaStreamSynchronize(s));
+    // the V-cycle recursion below the coarsest smoothed level uses lev[L-1] as the dense level
+}
+
+void mg_destroy(Handle& h) {
+    delete h.mg;
+    h.mg = nullptr;
+}
+
 }  // namespace eqc

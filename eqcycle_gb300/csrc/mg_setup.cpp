@@ -1,0 +1,237 @@
+// Host construction of the multigrid hierarchy (see mg.h): transfer tables, the vertex
+// operator A_1 = P_0^T K_II P_0 (element by element), Galerkin stencils of the coarser
+// vertex grids and the dense inverse of the coarsest operator.
+#include "mg.h"
+#include <cmath>
+#include <algorithm>
+
+namespace eqc {
+
+static void finish_restriction(Transfer1D& t) {
+    t.r_ptr.assign(t.nc + 1, 0);
+    for (int i = 0; i < t.nf; ++i)
+        for (int a = 0; a < 2; ++a)
+            if (t.p_w[2 * i + a] != 0.0) t.r_ptr[t.p_idx[2 * i + a] + 1]++;
+    for (int c = 0; c < t.nc; ++c) t.r_ptr[c + 1] += t.r_ptr[c];
+    t.r_idx.assign(t.r_ptr[t.nc], 0);
+    t.r_w.assign(t.r_ptr[t.nc], 0.0);
+    std::vector<int> pos(t.r_ptr.begin(), t.r_ptr.end() - 1);
+    for (int i = 0; i < t.nf; ++i)
+        for (int a = 0; a < 2; ++a)
+            if (t.p_w[2 * i + a] != 0.0) {
+                const int c = t.p_idx[2 * i + a];
+                t.r_idx[pos[c]] = i;
+                t.r_w[pos[c]] = t.p_w[2 * i + a];
+                pos[c]++;
+            }
+}
+
+// GLL lattice of nel elements (4*nel+1 points) -> the nel+1 element vertices:
+// linear interpolation in the element's reference coordinate t = (1+xi)/2.
+Transfer1D make_gll_transfer(int nel, const double* xgll) {
+    Transfer1D t;
+    t.nf = 4 * nel + 1;
+    t.nc = nel + 1;
+    t.p_idx.assign(2 * t.nf, 0);
+    t.p_w.assign(2 * t.nf, 0.0);
+    for (int i = 0; i < t.nf; ++i) {
+        const int e = std::min(i / 4, nel - 1);
+        const int k = i - 4 * e;
+        const double s = 0.5 * (1.0 + xgll[k]);
+        t.p_idx[2 * i] = e;
+        t.p_idx[2 * i + 1] = e + 1;
+        t.p_w[2 * i] = (k == 0) ? 1.0 : (k == 4 ? 0.0 : 1.0 - s);
+        t.p_w[2 * i + 1] = (k == 0) ? 0.0 : (k == 4 ? 1.0 : s);
+    }
+    finish_restriction(t);
+    return t;
+}
+
+// Factor-2 coarsening of nf points: coarse points at fine indices 0, 2, 4, ... and the last
+// fine index; fine points between two coarse points interpolate linearly by index.
+Transfer1D make_coarsen_transfer(int nf) {
+    std::vector<int> cpos;
+    for (int i = 0; i < nf; i += 2) cpos.push_back(i);
+    if (cpos.back() != nf - 1) cpos.push_back(nf - 1);
+    Transfer1D t;
+    t.nf = nf;
+    t.nc = (int)cpos.size();
+    t.p_idx.assign(2 * nf, 0);
+    t.p_w.assign(2 * nf, 0.0);
+    int c = 0;
+    for (int i = 0; i < nf; ++i) {
+        while (c + 1 < t.nc && cpos[c + 1] <= i) ++c;
+        if (cpos[c] == i) {
+            t.p_idx[2 * i] = c;
+            t.p_w[2 * i] = 1.0;
+            t.p_idx[2 * i + 1] = c;
+            t.p_w[2 * i + 1] = 0.0;
+        } else {
+            const double s = double(i - cpos[c]) / double(cpos[c + 1] - cpos[c]);
+            t.p_idx[2 * i] = c;
+            t.p_w[2 * i] = 1.0 - s;
+            t.p_idx[2 * i + 1] = c + 1;
+            t.p_w[2 * i + 1] = s;
+        }
+    }
+    finish_restriction(t);
+    return t;
+}
+
+// A_1 = P_0^T K_II P_0 on the (NelX+1) x (NelY+1) vertex grid, element by element: the
+// element operator (src/PCG.jl:82 form) applied to the four bilinear vertex functions.
+std::vector<double> vertex_operator(const Handle& h, const double* W) {
+    const Layout& L = h.L;
+    const int cx = L.NelX + 1, cy = L.NelY + 1;
+    std::vector<double> A((size_t)9 * cx * cy, 0.0);
+    const double* H = h.H;  // H[i + 5j] = h'_i(x_j)
+    double xg[5];
+    {   // GLL nodes are the zeros of the derivative matrix's row structure; recover them
+        // from H: x_j for a 5-point rule is -1, -sqrt(3/7), 0, sqrt(3/7), 1.
+        xg[0] = -1.0; xg[1] = -std::sqrt(3.0 / 7.0); xg[2] = 0.0; xg[3] = std::sqrt(3.0 / 7.0); xg[4] = 1.0;
+    }
+    double Lb[2][5];
+    for (int i = 0; i < 5; ++i) {
+        const double s = 0.5 * (1.0 + xg[i]);
+        Lb[0][i] = (i == 0) ? 1.0 : (i == 4 ? 0.0 : 1.0 - s);
+        Lb[1][i] = (i == 0) ? 0.0 : (i == 4 ? 1.0 : s);
+    }
+    for (int ey = 0; ey < L.NelY; ++ey)
+        for (int ex = 0; ex < L.NelX; ++ex) {
+            const double* w = W + ((int64_t)ey * L.NelX + ex) * 25;
+            double y[4][25];
+            for (int v = 0; v < 4; ++v) {
+                const int av = v & 1, bv = v >> 1;
+                double u[5][5], t1[5][5], t2[5][5];
+                for (int j = 0; j < 5; ++j)
+                    for (int i = 0; i < 5; ++i) u[i][j] = Lb[av][i] * Lb[bv][j];
+                for (int j = 0; j < 5; ++j)
+                    for (int p = 0; p < 5; ++p) {
+                        double s1 = 0, s2 = 0;
+                        for (int k = 0; k < 5; ++k) {
+                            s1 += H[k + 5 * p] * u[k][j];
+                            s2 += u[p][k] * H[k + 5 * j];
+                        }
+                        t1[p][j] = w[p + 5 * j] * s1;
+                        t2[p][j] = w[p + 5 * j] * s2;
+                    }
+                for (int j = 0; j < 5; ++j)
+                    for (int i = 0; i < 5; ++i) {
+                        double s1 = 0, s2 = 0;
+                        for (int p = 0; p < 5; ++p) {
+                            s1 += H[i + 5 * p] * t1[p][j];
+                            s2 += t2[i][p] * H[j + 5 * p];
+                        }
+                        y[v][i + 5 * j] = h.c1 * s1 + h.c2 * s2;
+                    }
+            }
+            for (int u = 0; u < 4; ++u) {
+                const int au = u & 1, bu = u >> 1;
+                const int vx = ex + au, vy = ey + bu;
+                for (int v = 0; v < 4; ++v) {
+                    const int av = v & 1, bv = v >> 1;
+                    double s = 0;
+                    for (int j = 0; j < 5; ++j)
+                        for (int i = 0; i < 5; ++i) s += Lb[au][i] * Lb[bu][j] * y[v][i + 5 * j];
+                    const int k = (bv - bu + 1) * 3 + (av - au + 1);
+                    A[(size_t)k * cx * cy + (size_t)vy * cx + vx] += s;
+                }
+            }
+        }
+    // fault row is Dirichlet: no equations on row 0, no couplings into row 0
+    for (int k = 0; k < 9; ++k)
+        for (int vx = 0; vx < cx; ++vx) A[(size_t)k * cx * cy + vx] = 0.0;
+    for (int vx = 0; vx < cx; ++vx)
+        for (int dx = -1; dx <= 1; ++dx) A[(size_t)((0) * 3 + (dx + 1)) * cx * cy + (size_t)1 * cx + vx] = 0.0;
+    return A;
+}
+
+// Galerkin product P^T A P for a 9-point stencil A on (cx, cy) and P = Py (x) Px.
+std::vector<double> galerkin_stencil(const std::vector<double>& A, int cx, int cy, const Transfer1D& tx,
+                                     const Transfer1D& ty, int ncx, int ncy) {
+    std::vector<double> Ac((size_t)9 * ncx * ncy, 0.0);
+    const size_t N = (size_t)cx * cy, Nc = (size_t)ncx * ncy;
+    for (int fy = 1; fy < cy; ++fy)
+        for (int fx = 0; fx < cx; ++fx) {
+            const size_t f = (size_t)fy * cx + fx;
+            for (int k = 0; k < 9; ++k) {
+                const double a = A[k * N + f];
+                if (a == 0.0) continue;
+                const int gx = fx + (k % 3) - 1, gy = fy + (k / 3) - 1;
+                if (gx < 0 || gx >= cx || gy < 1 || gy >= cy) continue;
+                for (int p = 0; p < 2; ++p)
+                    for (int q = 0; q < 2; ++q) {
+                        const double wJ = tx.p_w[2 * fx + p] * ty.p_w[2 * fy + q];
+                        if (wJ == 0.0) continue;
+                        const int Jx = tx.p_idx[2 * fx + p], Jy = ty.p_idx[2 * fy + q];
+                        if (Jy == 0) continue;
+                        for (int r = 0; r < 2; ++r)
+                            for (int s = 0; s < 2; ++s) {
+                                const double wK = tx.p_w[2 * gx + r] * ty.p_w[2 * gy + s];
+                                if (wK == 0.0) continue;
+                                const int Kx = tx.p_idx[2 * gx + r], Ky = ty.p_idx[2 * gy + s];
+                                if (Ky == 0) continue;
+                                const int dx = Kx - Jx, dy = Ky - Jy;
+                                if (dx < -1 || dx > 1 || dy < -1 || dy > 1)
+                                    throw Error(EQC_E_ARG, "Galerkin operator left the 9-point stencil");
+                                Ac[(size_t)((dy + 1) * 3 + dx + 1) * Nc + (size_t)Jy * ncx + Jx] += wJ * a * wK;
+                            }
+                    }
+            }
+        }
+    return Ac;
+}
+
+// Dense inverse of the SPD operator on rows >= 1 of a small grid (Cholesky).
+std::vector<double> dense_inverse_spd(const std::vector<double>& A9, int cx, int cy, int& n) {
+    n = cx * (cy - 1);
+    const size_t N = (size_t)cx * cy;
+    std::vector<double> M((size_t)n * n, 0.0);
+    for (int iy = 1; iy < cy; ++iy)
+        for (int ix = 0; ix < cx; ++ix) {
+            const int r = (iy - 1) * cx + ix;
+            for (int k = 0; k < 9; ++k) {
+                const int gx = ix + (k % 3) - 1, gy = iy + (k / 3) - 1;
+                if (gx < 0 || gx >= cx || gy < 1 || gy >= cy) continue;
+                M[(size_t)r * n + (gy - 1) * cx + gx] += A9[k * N + (size_t)iy * cx + ix];
+            }
+        }
+    // symmetrise round-off, Cholesky M = L L^T (lower, in place)
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < i; ++j) {
+            const double s = 0.5 * (M[(size_t)i * n + j] + M[(size_t)j * n + i]);
+            M[(size_t)i * n + j] = M[(size_t)j * n + i] = s;
+        }
+    std::vector<double> Lm(M);
+    for (int j = 0; j < n; ++j) {
+        double d = Lm[(size_t)j * n + j];
+        for (int k = 0; k < j; ++k) d -= Lm[(size_t)j * n + k] * Lm[(size_t)j * n + k];
+        if (!(d > 0)) throw Error(EQC_E_ARG, "coarsest multigrid operator is not positive definite");
+        d = std::sqrt(d);
+        Lm[(size_t)j * n + j] = d;
+        for (int i = j + 1; i < n; ++i) {
+            double s = Lm[(size_t)i * n + j];
+            for (int k = 0; k < j; ++k) s -= Lm[(size_t)i * n + k] * Lm[(size_t)j * n + k];
+            Lm[(size_t)i * n + j] = s / d;
+        }
+    }
+    std::vector<double> Inv((size_t)n * n, 0.0), col(n);
+    for (int c = 0; c < n; ++c) {
+        std::fill(col.begin(), col.end(), 0.0);
+        col[c] = 1.0;
+        for (int i = 0; i < n; ++i) {  // L y = e_c
+            double s = col[i];
+            for (int k = 0; k < i; ++k) s -= Lm[(size_t)i * n + k] * col[k];
+            col[i] = s / Lm[(size_t)i * n + i];
+        }
+        for (int i = n - 1; i >= 0; --i) {  // L^T x = y
+            double s = col[i];
+            for (int k = i + 1; k < n; ++k) s -= Lm[(size_t)k * n + i] * col[k];
+            col[i] = s / Lm[(size_t)i * n + i];
+        }
+        for (int i = 0; i < n; ++i) Inv[(size_t)i * n + c] = col[i];
+    }
+    return Inv;
+}
+
+}  // namespace eqc

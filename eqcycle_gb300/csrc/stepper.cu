@@ -468,6 +468,10 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
     const int64_t cg0 = h.cg_iters_total, qs0 = h.qs_solves_total;
     std::vector<double> dF, vF, tauF, seis(3 * std::max(h.nSeis, 1));
     Ctrl& C = *h.h_ctrl;
+    cudaEvent_t ev0, ev1;
+    EQC_CUDA(cudaEventCreate(&ev0));
+    EQC_CUDA(cudaEventCreate(&ev1));
+    EQC_CUDA(cudaEventRecord(ev0, s));
     while (C.t < t_end && stats.steps < max_steps) {
         // it = it + 1 ; t = t + dt (main.jl:221-222); dt of this step is C.dt
         C.it += 1;
@@ -609,6 +613,13 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
         h.res.Vfmax.push_back(Vfmax);
         stats.steps++;
     }
+    EQC_CUDA(cudaEventRecord(ev1, s));
+    EQC_CUDA(cudaEventSynchronize(ev1));
+    float gms = 0.f;
+    EQC_CUDA(cudaEventElapsedTime(&gms, ev0, ev1));
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    stats.gpu_ms = gms;
     stats.cg_iters = h.cg_iters_total - cg0;
     stats.qs_solves = h.qs_solves_total - qs0;
     stats.t = C.t;

@@ -177,6 +177,9 @@ class Solver:
         self._chk(L.lib().eqc_get_scalar(self.h, name.encode(), C.byref(out)))
         return out.value
 
+    def set_scalar(self, name: str, value: float):
+        self._chk(L.lib().eqc_set_scalar(self.h, name.encode(), float(value)))
+
     def result(self, field: str) -> np.ndarray:
         n = L.lib().eqc_result_size(self.h, field.encode())
         if n < 0:

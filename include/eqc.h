@@ -140,6 +140,8 @@ typedef struct {
     int32_t isolver;       /* regime for the next step (1 QS, 2 dynamic) */
     int32_t events;        /* events started so far               */
     double wall_s;         /* wall time spent in this call        */
+    double gpu_ms;         /* CUDA-event time on the handle's stream between the first
+                              and the last kernel of this call     */
 } eqc_run_stats;
 
 /* Advance the time loop until t >= t_end or max_steps steps were taken.  The
@@ -150,8 +152,10 @@ eqc_status eqc_run(eqc_handle* h, int64_t max_steps, double t_end, eqc_run_stats
  * [nglob], "psi", "tau" [FltNglob].  eqc_set_state writes it back. */
 eqc_status eqc_get_state(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
-/* Scalars "t", "dt", "isolver", "it". */
+/* Scalars "t", "dt", "isolver", "it" (and, read-only, "cg_iters", "qs_solves").
+ * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
+eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);
 
 /* Results of main.jl:479-498, trimmed as in main.jl:455-472.  eqc_result_size
  * gives the element count of a field (fault-major matrices are FltNglob x n,

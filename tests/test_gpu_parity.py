@@ -140,3 +140,25 @@ def test_mixed_precision_qs_solve(models, oracle_mod):
         d, it, rr = s.qs_solve(F, d0, tol=1e-8)
     assert it > 0 and rr <= 1e-8        # certified on the FP64 true residual
     assert rel(d, d_ref) <= 1e-5
+
+
+@pytest.mark.parametrize("precision", [EQC_FP64, EQC_MIXED], ids=["fp64", "mixed"])
+def test_multigrid_qs_solve_matches_oracle(models, oracle_mod, precision):
+    """Multigrid-preconditioned CG: converged solution equals the oracle's, in few iterations."""
+    cfg, P, o = models["dz40"]
+    rng = np.random.default_rng(6)
+    F = rng.uniform(0, 1e-2, P.int_.FltNglob)
+    d0 = rng.uniform(-1e-3, 1e-3, P.int_.nglob)
+    d_ref, _, _ = o.qs_solve(F, d0, tol=1e-13, mode=1)
+    tol = 1e-13 if precision == EQC_FP64 else 1e-10
+    with Solver(P, precision=precision, precond=EQC_PC_AMG) as s:
+        d, it, rr = s.qs_solve(F, d0, tol=tol)
+    assert 0 < it <= 40 and rr <= tol
+    assert rel(d, d_ref) <= (1e-10 if precision == EQC_FP64 else 1e-7)
+
+
+def test_multigrid_time_loop_matches_oracle(eqclib, oracle_mod):
+    P, o, st, got, ref, res = _run_both(reference_config(res=1), 30, oracle_mod, 1e-14, precond=EQC_PC_AMG)
+    assert st["steps"] == 30
+    for k in ("d", "v", "psi", "tau"):
+        assert rel(got[k], ref[k]) <= 1e-8, k
