@@ -61,7 +61,7 @@ _lib: Optional[C.CDLL] = None
 
 # Every symbol include/eqc.h declares (checked by the CPU test suite).
 EXPORTS = ["eqc_default_options", "eqc_create", "eqc_destroy", "eqc_last_error", "eqc_apply_K", "eqc_qs_solve",
-           "eqc_slrFunc", "eqc_FBC", "eqc_dtevol", "eqc_init", "eqc_run", "eqc_get_state", "eqc_set_state",
+           "eqc_slrFunc", "eqc_FBC", "eqc_dtevol", "eqc_dtevol_noalloc", "eqc_init", "eqc_run", "eqc_get_state", "eqc_set_state",
            "eqc_get_scalar", "eqc_set_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
            "eqc_time_apply", "eqc_launch_count", "eqc_sync"]
 
@@ -86,6 +86,7 @@ def lib() -> C.CDLL:
     L.eqc_slrFunc.argtypes = [P, _dp, _dp, _dp, _dp, _dp, D]
     L.eqc_FBC.argtypes = [P] + [_dp] * 9 + [D, _ip]
     L.eqc_dtevol.argtypes = [P, D, D, _dp, I32, _dp]
+    L.eqc_dtevol_noalloc.argtypes = [P, P, I64, I64, D, D, I32, P, P]
     L.eqc_init.argtypes = [P, D]
     L.eqc_run.argtypes = [P, I64, D, C.POINTER(EqcRunStats)]
     L.eqc_get_state.argtypes = [P, C.c_char_p, _dp]

@@ -204,6 +204,9 @@ static void from_layout(const Handle& h, const std::vector<double>& lay, double*
     for (int64_t g = 0; g < h.nglob; ++g) ref[g] = lay[h.ref2lay[g]];
 }
 
+static thread_local std::string g_create_err;
+void set_thread_error(const std::string& msg) { g_create_err = msg; }
+
 }  // namespace eqc
 
 using namespace eqc;
@@ -238,7 +241,6 @@ void eqc_default_options(eqc_options* o) {
     o->verbose = 0;
 }
 
-static thread_local std::string g_create_err;
 
 eqc_status eqc_create(const eqc_model* model, const eqc_options* opt, eqc_handle** out) {
     if (!model || !out) return EQC_E_ARG;

@@ -95,6 +95,9 @@ struct ApplyArgs {
     Layout L;
 };
 
+// Error text for entry points without a handle (returned by eqc_last_error(NULL)).
+void set_thread_error(const std::string& msg);
+
 // Kernel counters (what the library launched).
 extern int64_t g_launches;
 inline void count_launch(int n = 1) { g_launches += n; }

@@ -124,6 +124,24 @@ eqc_status eqc_FBC(eqc_handle* h, double* psi1, double* Vf1, double* tau1, doubl
 eqc_status eqc_dtevol(eqc_handle* h, double dt, double dtmin, const double* Vf,
                       int32_t isolver, double* dt_out);
 
+/* Largest fault-node count eqc_dtevol_noalloc accepts. */
+#define EQC_NOALLOC_MAX_NODES (1 << 22)
+
+/* No counterpart in the reference.  The time step of eqc_dtevol, for callers that
+ * cannot allocate device memory (a host code that owns a fixed device arena, an
+ * allocator budget that forbids library cudaMalloc, a call site where allocation
+ * would synchronise the device): it needs no handle and allocates nothing.  Vf and
+ * XiLf are the caller's device arrays of n fault nodes, NFBC the 1-based first
+ * friction node (src/main.jl:186), dt_out a device double written on `stream`
+ * (a cudaStream_t, NULL for the default stream).  n may not exceed
+ * EQC_NOALLOC_MAX_NODES (EQC_E_ARG otherwise; message in eqc_last_error(NULL)).
+ * The reduction scratch is a fixed static device array shared by every call: calls
+ * that overlap on the GPU race on it.  The first call on a device looks up that
+ * array's device address; make it before any stream capture. */
+eqc_status eqc_dtevol_noalloc(const double* Vf, const double* XiLf, int64_t n, int64_t NFBC,
+                              double dt, double dtmin, int32_t isolver, double* dt_out,
+                              void* stream);
+
 /* ---- the time loop (src/main.jl:67-477) ------------------------------------- */
 
 /* Initial state of main.jl:89-190 with v = V_init/2 (main.jl:102 uses
