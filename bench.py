@@ -295,6 +295,24 @@ def bench_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_kernel(args):
+    """Stiffness apply alone on the workload mesh, L2 flushed between launches."""
+    from eqcycle_gb300 import EQC_PC_JACOBI, Solver, preset, set_parameters
+    P = set_parameters(preset(args.workload))
+    nglob, Nel = P.int_.nglob, P.int_.Nel
+    peak, kind = measured_peaks()
+    with Solver(P, precond=EQC_PC_JACOBI) as s:
+        out = {"workload": args.workload, "nodes": nglob, "elements": Nel, "peak_gbs": peak, "peak_kind": kind}
+        for name, dt, es in (("f32", 1, 4), ("f64", 0, 8)):
+            if args.dtype not in ("both", name):
+                continue
+            ms = s.time_apply(dt, args.nrep, True)
+            B = es * (2 * nglob + 25 * Nel)
+            out[name] = {"launch_us": ms * 1e3, "algorithmic_bytes": B, "achieved_gbs": B / ms / 1e6,
+                         "frac": B / ms / 1e6 / peak}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -304,8 +322,13 @@ def main():
     ap.add_argument("--workload", default="dz480")
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true", help="time the stiffness apply alone")
+    ap.add_argument("--dtype", default="both", choices=["both", "f32", "f64"])
+    ap.add_argument("--nrep", type=int, default=20)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.kernel_only:
+        bench_kernel(args)
+    elif args.impl == "reference":
         bench_reference(args)
     else:
         bench_ours(args)

@@ -55,7 +55,7 @@ static void create(Handle& h, const eqc_model& m) {
     L.NelY = (int)m.NelY;
     L.nx = 4 * L.NelX + 1;
     L.ny = 4 * L.NelY + 1;
-    L.ld = L.nx;
+    L.ld = (L.nx + 7) / 8 * 8;   // rows start on 32-byte (FP32) / 64-byte (FP64) boundaries
     h.nglob = m.nglob;
     h.Nel = m.Nel;
     h.dxe = m.dxe;
@@ -108,7 +108,8 @@ static void create(Handle& h, const eqc_model& m) {
     for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32}) b->alloc(N);
     h.M.upload(Mlay.data(), N, s);
     std::vector<double> dg = diag_K(h, m.W);
-    for (int64_t i = 0; i < L.ld; ++i) dg[i] = 1.0;  // fault row is not part of the system
+    for (int64_t i = 0; i < N; ++i)   // fault row and row padding are not part of the system
+        if (i < L.ld || (i % L.ld) >= L.nx) dg[i] = 1.0;
     std::vector<float> dg32(dg.begin(), dg.end());
     h.diag64.alloc(N);
     h.diag64.upload(dg.data(), N, s);

@@ -156,6 +156,149 @@ __global__ void __launch_bounds__(256) k_apply(const T* __restrict__ x, T* __res
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Full apply (modes 0 and 1), node-line formulation.
+//
+// For a node row iy the x-derivative part of K x is, element column by element column,
+//   y1 = c1 * H * (Wrow .* (H' u_row))   with Wrow[p] = sum over the element rows holding iy
+// of W_e[p, j_e] (one row inside an element, two on an element boundary: the operator is
+// linear in W, so the two element rows collapse into one line).  Likewise every node column
+// gives one y-line with the summed W column.  A CTA owns nodes [4ex0, 4ex0+4TEX) x
+// [4ey0, 4ey0+4TEY) and runs one x-line item per (owned node row, element column incl. the
+// left halo element) and one y-line item per (owned node column, element row incl. the
+// bottom halo element).  An item writes its 4 owned outputs and hands the 5th (the shared
+// endpoint, owned by the neighbour item) through a small shared array; the final pass adds
+// those carries in a fixed order (deterministic, no atomics).  Elements outside the mesh
+// act as W = 0, so the one extra CTA row/column that owns the last node line needs no
+// special case.
+template <class T, int TEX, int TEY, int NT>
+__global__ void __launch_bounds__(NT) k_apply_lines(const T* __restrict__ x, T* __restrict__ y, ApplyArgs<T> A,
+                                                    T sign, int zero_row0) {
+    const Layout L = A.L;
+    constexpr int UX = 4 * TEX + 5, UY = 4 * TEY + 5;   // node tile incl. one halo element
+    constexpr int OX = 4 * TEX, OY = 4 * TEY;           // owned nodes
+    constexpr int EX = TEX + 1, EY = TEY + 1;           // elements incl. halo
+    __shared__ T us[UY * UX];
+    __shared__ T ws[EY * EX * 25];
+    __shared__ T ys[OY * OX];
+    __shared__ T cx[OY * EX];   // x-line endpoint carries [row][element column]
+    __shared__ T cy[EY * OX];   // y-line endpoint carries [element row][column]
+    const int ex0 = blockIdx.x * TEX, ey0 = blockIdx.y * TEY;
+    const int ix0 = 4 * ex0 - 4, iy0 = 4 * ey0 - 4;
+
+    // Issue every tile load of this thread before the first shared-memory store, so that
+    // all of them are in flight together (compile-time trip counts, predicated).
+    constexpr int NU = (UY * UX + NT - 1) / NT, NWL = (EY * EX * 25 + NT - 1) / NT;
+    T ur[NU], wr[NWL];
+#pragma unroll
+    for (int it = 0; it < NU; ++it) {
+        const int k = threadIdx.x + it * NT;
+        const int b = k / UX, a = k - b * UX;
+        const int ix = ix0 + a, iy = iy0 + b;
+        ur[it] = (k < UY * UX && ix >= 0 && ix < L.nx && iy >= 0 && iy < L.ny) ? __ldg(x + (int64_t)iy * L.ld + ix)
+                                                                                : T(0);
+    }
+#pragma unroll
+    for (int it = 0; it < NWL; ++it) {
+        const int k = threadIdx.x + it * NT;
+        const int le = k / 25, q = k - le * 25;
+        const int er = le / EX, ec = le - er * EX;
+        const int ex = ex0 - 1 + ec, ey = ey0 - 1 + er;
+        wr[it] = (k < EY * EX * 25 && ex >= 0 && ex < L.NelX && ey >= 0 && ey < L.NelY)
+                     ? __ldg(A.W + ((int64_t)ey * L.NelX + ex) * 25 + q)
+                     : T(0);
+    }
+#pragma unroll
+    for (int it = 0; it < NU; ++it) {
+        const int k = threadIdx.x + it * NT;
+        if (k < UY * UX) us[k] = ur[it];
+    }
+#pragma unroll
+    for (int it = 0; it < NWL; ++it) {
+        const int k = threadIdx.x + it * NT;
+        if (k < EY * EX * 25) ws[k] = wr[it];
+    }
+    __syncthreads();
+
+    // x-lines: item = (owned node row r, element column c = 0..TEX, c = 0 the left halo)
+    for (int t = threadIdx.x; t < OY * EX; t += NT) {
+        const int r = t / EX, c = t - r * EX;
+        const int er = (r >> 2) + 1, j = r & 3;
+        const T* ul = us + (r + 4) * UX + 4 * c;
+        const T* w1 = ws + (er * EX + c) * 25 + 5 * j;
+        const T* w0 = ws + ((er - 1) * EX + c) * 25 + 20;
+        T u[5], s[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) u[k] = ul[k];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc += Hc<T>(k, p) * u[k];
+            const T wr = (j == 0) ? w1[p] + w0[p] : w1[p];
+            s[p] = wr * acc;
+        }
+        T o[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            T acc = T(0);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += Hc<T>(i, p) * s[p];
+            o[i] = A.c1 * acc;
+        }
+        if (c > 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) ys[r * OX + 4 * (c - 1) + i] = o[i];
+        }
+        cx[r * EX + c] = o[4];
+    }
+    __syncthreads();
+    // y-lines: item = (owned node column q, element row er = 0..TEY, er = 0 the bottom halo)
+    for (int t = threadIdx.x; t < EY * OX; t += NT) {
+        const int er = t / OX, q = t - er * OX;
+        const int ec = (q >> 2) + 1, i = q & 3;
+        const T* ul = us + (4 * er) * UX + q + 4;
+        const T* w1 = ws + (er * EX + ec) * 25 + i;
+        const T* w0 = ws + (er * EX + ec - 1) * 25 + 4;
+        T u[5], s[5];
+#pragma unroll
+        for (int l = 0; l < 5; ++l) u[l] = ul[l * UX];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            T acc = T(0);
+#pragma unroll
+            for (int l = 0; l < 5; ++l) acc += u[l] * Hc<T>(l, p);
+            const T wc = (i == 0) ? w1[5 * p] + w0[5 * p] : w1[5 * p];
+            s[p] = wc * acc;
+        }
+        T o[5];
+#pragma unroll
+        for (int jj = 0; jj < 5; ++jj) {
+            T acc = T(0);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += s[p] * Hc<T>(jj, p);
+            o[jj] = A.c2 * acc;
+        }
+        if (er > 0) {
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) ys[(4 * (er - 1) + jj) * OX + q] += o[jj];
+        }
+        cy[er * OX + q] = o[4];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < OY * OX; k += NT) {
+        const int r = k / OX, q = k - r * OX;
+        const int ix = 4 * ex0 + q, iy = 4 * ey0 + r;
+        if (ix >= L.nx || iy >= L.ny) continue;
+        T v = ys[k];
+        if ((q & 3) == 0) v += cx[r * EX + (q >> 2)];
+        if ((r & 3) == 0) v += cy[(r >> 2) * OX + q];
+        v = sign * v;
+        if (zero_row0 && iy == 0) v = T(0);
+        y[(int64_t)iy * L.ld + ix] = v;
+    }
+}
+
 constexpr int TEX = 8, TEY = 8;
 
 template <class T>
@@ -163,8 +306,17 @@ static size_t apply_smem() {
     return sizeof(T) * ((size_t)(4 * (TEX + 1) + 1) * (4 * (TEY + 1) + 1) + 2 * (size_t)(TEX + 1) * (TEY + 1) * 25);
 }
 
+constexpr int LTEX = 8, LTEY = 7, LNT = 256;
+
 template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s) {
+    if (mode <= 1) {
+        dim3 grid(A.L.NelX / LTEX + 1, A.L.NelY / LTEY + 1);
+        k_apply_lines<T, LTEX, LTEY, LNT><<<grid, LNT, 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+        return;
+    }
     static bool attr_set = false;
     const size_t sm = apply_smem<T>();
     if (!attr_set) {

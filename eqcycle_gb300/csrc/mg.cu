@@ -303,7 +303,8 @@ static double estimate_lmax(Handle& h, int l) {
     std::mt19937_64 rng(1234 + l);
     std::uniform_real_distribution<double> U(0.5, 1.5);
     const int nx = (l == 0) ? h.L.ld : m.lev[l - 1].cx;
-    for (int64_t i = 0; i < n; ++i) x0[i] = (i < nx) ? 0.0 : U(rng);
+    const int nreal = (l == 0) ? h.L.nx : nx;
+    for (int64_t i = 0; i < n; ++i) x0[i] = (i < nx || (i % nx) >= nreal) ? 0.0 : U(rng);
     w.x64.upload(x0.data(), n, h.stream);
     double lam = 0.0;
     for (int it = 0; it < 30; ++it) {
