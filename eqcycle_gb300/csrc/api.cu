@@ -98,6 +98,20 @@ static void create(Handle& h, const eqc_model& m) {
     for (size_t k = 0; k < nW; ++k) w32[k] = (float)m.W[k];
     h.W32.alloc(nW);
     h.W32.upload(w32.data(), nW, s);
+    {   // copies padded per element for TMA element tiles
+        const int p32 = WPad<float>::v, p64 = WPad<double>::v;
+        std::vector<float> a((size_t)p32 * m.Nel, 0.f);
+        std::vector<double> b((size_t)p64 * m.Nel, 0.0);
+        for (int64_t e = 0; e < m.Nel; ++e)
+            for (int q = 0; q < 25; ++q) {
+                a[(size_t)p32 * e + q] = w32[(size_t)25 * e + q];
+                b[(size_t)p64 * e + q] = m.W[(size_t)25 * e + q];
+            }
+        h.W32p.alloc(a.size());
+        h.W32p.upload(a.data(), a.size(), s);
+        h.W64p.alloc(b.size());
+        h.W64p.upload(b.data(), b.size(), s);
+    }
 
     // node arrays
     const int64_t N = L.size();
@@ -187,6 +201,8 @@ static void create(Handle& h, const eqc_model& m) {
 
     // control, reductions
     h.ctrl.alloc(1);
+    EQC_CUDA(cudaStreamSynchronize(s));
+    tma_init(h);
     EQC_CUDA(cudaMallocHost(&h.h_ctrl, sizeof(Ctrl)));
     std::memset(h.h_ctrl, 0, sizeof(Ctrl));
     h.red_part.alloc(4096);

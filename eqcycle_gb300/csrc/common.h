@@ -1,7 +1,9 @@
 // Internal definitions of libeqc (GB300 / sm_103a implementation of the eqcycle hot path).
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda.h>
 #include <cstdint>
+#include <unordered_map>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -86,6 +88,19 @@ struct Layout {
     __host__ __device__ int64_t interior_begin() const { return ld; }   // first entry of row 1
 };
 
+// TMA tensor maps of the stiffness apply: one per node vector (keyed by its address) and
+// one for the padded element data, per precision.
+struct TmaCache {
+    bool ok = false;
+    std::unordered_map<const void*, CUtensorMap> u32, u64;
+    CUtensorMap w32, w64;
+};
+
+// W padded to a 16-byte multiple per element, so element tiles are TMA-addressable.
+template <class T> struct WPad;
+template <> struct WPad<float> { static constexpr int v = 28; };
+template <> struct WPad<double> { static constexpr int v = 26; };
+
 // Stiffness apply parameters (element data in the reference's [i,j,e] layout,
 // element e = ey*NelX + ex, src/MaterialProperties.jl:9).
 template <class T>
@@ -93,6 +108,9 @@ struct ApplyArgs {
     const T* W;       // [25*Nel]
     T c1, c2;         // coefint1, coefint2 (par.jl:35-36)
     Layout L;
+    const T* Wp;      // [WPad*Nel] padded copy for TMA (may be null)
+    int* err;         // device flag set when a bounded wait gives up (may be null)
+    TmaCache* tma;    // host-side tensor-map cache (may be null)
 };
 
 // Error text for entry points without a handle (returned by eqc_last_error(NULL)).

@@ -13,7 +13,8 @@
 // the tile are recomputed as a halo.  Per element the work is split into 5 x-lines
 // and 5 y-lines (sum factorisation: two 5x5 contractions per line) staged through
 // shared memory.
-#include "common.h"
+#include "model.h"
+#include <cstdlib>
 
 namespace eqc {
 
@@ -171,6 +172,94 @@ __global__ void __launch_bounds__(256) k_apply(const T* __restrict__ x, T* __res
 // those carries in a fixed order (deterministic, no atomics).  Elements outside the mesh
 // act as W = 0, so the one extra CTA row/column that owns the last node line needs no
 // special case.
+// Line items and output pass shared by both full-apply kernels.  us: node tile with row
+// pitch UP; ws: element tile, element stride WP, EX elements per row.
+template <class T, int TEX, int TEY, int NT, int UP, int WP>
+__device__ __forceinline__ void lines_compute(const T* __restrict__ us, const T* __restrict__ ws, T* ys, T* cx,
+                                              T* cy, T* __restrict__ y, const ApplyArgs<T>& A, int ex0, int ey0,
+                                              T sign, int zero_row0) {
+    const Layout& L = A.L;
+    constexpr int OX = 4 * TEX, OY = 4 * TEY;
+    constexpr int EX = TEX + 1, EY = TEY + 1;
+    // x-lines: item = (owned node row r, element column c = 0..TEX, c = 0 the left halo)
+    for (int t = threadIdx.x; t < OY * EX; t += NT) {
+        const int r = t / EX, c = t - r * EX;
+        const int er = (r >> 2) + 1, j = r & 3;
+        const T* ul = us + (r + 4) * UP + 4 * c;
+        const T* w1 = ws + (er * EX + c) * WP + 5 * j;
+        const T* w0 = ws + ((er - 1) * EX + c) * WP + 20;
+        T u[5], s[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) u[k] = ul[k];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc += Hc<T>(k, p) * u[k];
+            const T wr = (j == 0) ? w1[p] + w0[p] : w1[p];
+            s[p] = wr * acc;
+        }
+        T o[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            T acc = T(0);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += Hc<T>(i, p) * s[p];
+            o[i] = A.c1 * acc;
+        }
+        if (c > 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) ys[r * OX + 4 * (c - 1) + i] = o[i];
+        }
+        cx[r * EX + c] = o[4];
+    }
+    __syncthreads();
+    // y-lines: item = (owned node column q, element row er = 0..TEY, er = 0 the bottom halo)
+    for (int t = threadIdx.x; t < EY * OX; t += NT) {
+        const int er = t / OX, q = t - er * OX;
+        const int ec = (q >> 2) + 1, i = q & 3;
+        const T* ul = us + (4 * er) * UP + q + 4;
+        const T* w1 = ws + (er * EX + ec) * WP + i;
+        const T* w0 = ws + (er * EX + ec - 1) * WP + 4;
+        T u[5], s[5];
+#pragma unroll
+        for (int l = 0; l < 5; ++l) u[l] = ul[l * UP];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            T acc = T(0);
+#pragma unroll
+            for (int l = 0; l < 5; ++l) acc += u[l] * Hc<T>(l, p);
+            const T wc = (i == 0) ? w1[5 * p] + w0[5 * p] : w1[5 * p];
+            s[p] = wc * acc;
+        }
+        T o[5];
+#pragma unroll
+        for (int jj = 0; jj < 5; ++jj) {
+            T acc = T(0);
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += s[p] * Hc<T>(jj, p);
+            o[jj] = A.c2 * acc;
+        }
+        if (er > 0) {
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) ys[(4 * (er - 1) + jj) * OX + q] += o[jj];
+        }
+        cy[er * OX + q] = o[4];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < OY * OX; k += NT) {
+        const int r = k / OX, q = k - r * OX;
+        const int ix = 4 * ex0 + q, iy = 4 * ey0 + r;
+        if (ix >= L.nx || iy >= L.ny) continue;
+        T v = ys[k];
+        if ((q & 3) == 0) v += cx[r * EX + (q >> 2)];
+        if ((r & 3) == 0) v += cy[(r >> 2) * OX + q];
+        v = sign * v;
+        if (zero_row0 && iy == 0) v = T(0);
+        y[(int64_t)iy * L.ld + ix] = v;
+    }
+}
+
 template <class T, int TEX, int TEY, int NT>
 __global__ void __launch_bounds__(NT) k_apply_lines(const T* __restrict__ x, T* __restrict__ y, ApplyArgs<T> A,
                                                     T sign, int zero_row0) {
@@ -220,83 +309,108 @@ __global__ void __launch_bounds__(NT) k_apply_lines(const T* __restrict__ x, T* 
     }
     __syncthreads();
 
-    // x-lines: item = (owned node row r, element column c = 0..TEX, c = 0 the left halo)
-    for (int t = threadIdx.x; t < OY * EX; t += NT) {
-        const int r = t / EX, c = t - r * EX;
-        const int er = (r >> 2) + 1, j = r & 3;
-        const T* ul = us + (r + 4) * UX + 4 * c;
-        const T* w1 = ws + (er * EX + c) * 25 + 5 * j;
-        const T* w0 = ws + ((er - 1) * EX + c) * 25 + 20;
-        T u[5], s[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) u[k] = ul[k];
-#pragma unroll
-        for (int p = 0; p < 5; ++p) {
-            T acc = T(0);
-#pragma unroll
-            for (int k = 0; k < 5; ++k) acc += Hc<T>(k, p) * u[k];
-            const T wr = (j == 0) ? w1[p] + w0[p] : w1[p];
-            s[p] = wr * acc;
-        }
-        T o[5];
-#pragma unroll
-        for (int i = 0; i < 5; ++i) {
-            T acc = T(0);
-#pragma unroll
-            for (int p = 0; p < 5; ++p) acc += Hc<T>(i, p) * s[p];
-            o[i] = A.c1 * acc;
-        }
-        if (c > 0) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) ys[r * OX + 4 * (c - 1) + i] = o[i];
-        }
-        cx[r * EX + c] = o[4];
+    lines_compute<T, TEX, TEY, NT, UX, 25>(us, ws, ys, cx, cy, y, A, ex0, ey0, sign, zero_row0);
+}
+
+// ---- TMA version -------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// 2-D tiled bulk tensor load global -> shared, completion counted on the mbarrier.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+constexpr int UPT = 40;                    // node-tile row pitch of the TMA box (16-byte multiple)
+constexpr int MBAR_SPIN_LIMIT = 1 << 22;   // bounded wait on the TMA barrier
+
+// Full apply with the node tile and the element tile fetched by TMA.  The node box starts at
+// x = 4*ex0 - 4 (a multiple of 4 elements, hence 16-byte aligned) and the hardware fills
+// coordinates outside the grid with zeros; the element box starts at element ex0 - 1 of a
+// copy of W padded to WPad values per element.
+template <class T, int TEX, int TEY, int NT>
+__global__ void __launch_bounds__(NT) k_apply_tma(const __grid_constant__ CUtensorMap umap,
+                                                  const __grid_constant__ CUtensorMap wmap, T* __restrict__ y,
+                                                  ApplyArgs<T> A, T sign, int zero_row0) {
+    constexpr int UY = 4 * TEY + 5;
+    constexpr int OX = 4 * TEX, OY = 4 * TEY;
+    constexpr int EX = TEX + 1, EY = TEY + 1;
+    constexpr int WP = WPad<T>::v;
+    __shared__ __align__(128) T us[UY * UPT];
+    __shared__ __align__(128) T ws[EY * EX * WP];
+    __shared__ T ys[OY * OX];
+    __shared__ T cx[OY * EX];
+    __shared__ T cy[EY * OX];
+    __shared__ __align__(8) uint64_t bar;
+    const int ex0 = blockIdx.x * TEX, ey0 = blockIdx.y * TEY;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
     }
     __syncthreads();
-    // y-lines: item = (owned node column q, element row er = 0..TEY, er = 0 the bottom halo)
-    for (int t = threadIdx.x; t < EY * OX; t += NT) {
-        const int er = t / OX, q = t - er * OX;
-        const int ec = (q >> 2) + 1, i = q & 3;
-        const T* ul = us + (4 * er) * UX + q + 4;
-        const T* w1 = ws + (er * EX + ec) * 25 + i;
-        const T* w0 = ws + (er * EX + ec - 1) * 25 + 4;
-        T u[5], s[5];
-#pragma unroll
-        for (int l = 0; l < 5; ++l) u[l] = ul[l * UX];
-#pragma unroll
-        for (int p = 0; p < 5; ++p) {
-            T acc = T(0);
-#pragma unroll
-            for (int l = 0; l < 5; ++l) acc += u[l] * Hc<T>(l, p);
-            const T wc = (i == 0) ? w1[5 * p] + w0[5 * p] : w1[5 * p];
-            s[p] = wc * acc;
-        }
-        T o[5];
-#pragma unroll
-        for (int jj = 0; jj < 5; ++jj) {
-            T acc = T(0);
-#pragma unroll
-            for (int p = 0; p < 5; ++p) acc += s[p] * Hc<T>(jj, p);
-            o[jj] = A.c2 * acc;
-        }
-        if (er > 0) {
-#pragma unroll
-            for (int jj = 0; jj < 4; ++jj) ys[(4 * (er - 1) + jj) * OX + q] += o[jj];
-        }
-        cy[er * OX + q] = o[4];
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, (uint32_t)(sizeof(T) * (UY * UPT + EY * EX * WP)));
+        tma_load_2d(us, &umap, &bar, 4 * ex0 - 4, 4 * ey0 - 4);
+        tma_load_2d(ws, &wmap, &bar, (ex0 - 1) * WP, ey0 - 1);
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < OY * OX; k += NT) {
-        const int r = k / OX, q = k - r * OX;
-        const int ix = 4 * ex0 + q, iy = 4 * ey0 + r;
-        if (ix >= L.nx || iy >= L.ny) continue;
-        T v = ys[k];
-        if ((q & 3) == 0) v += cx[r * EX + (q >> 2)];
-        if ((r & 3) == 0) v += cy[(r >> 2) * OX + q];
-        v = sign * v;
-        if (zero_row0 && iy == 0) v = T(0);
-        y[(int64_t)iy * L.ld + ix] = v;
+    bool done = false;
+    for (int it = 0; it < MBAR_SPIN_LIMIT && !done; ++it) done = mbar_try_wait(&bar, 0);
+    if (!done) {
+        // give up: flag it, wait (bounded) for the copies still targeting this CTA, leave
+        if (threadIdx.x == 0 && A.err) atomicExch(A.err, 1);
+        for (int it = 0; it < MBAR_SPIN_LIMIT; ++it)
+            if (mbar_try_wait(&bar, 0)) break;
+        return;
     }
+    lines_compute<T, TEX, TEY, NT, UPT, WP>(us, ws, ys, cx, cy, y, A, ex0, ey0, sign, zero_row0);
+}
+
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static PFN_encodeTiled encode_fn() {
+    static PFN_encodeTiled fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_encodeTiled)p;
+    }
+    return fn;
+}
+
+static bool encode_2d(CUtensorMap* m, bool f64, const void* base, uint64_t d0, uint64_t d1, uint64_t stride_bytes,
+                      uint32_t b0, uint32_t b1) {
+    PFN_encodeTiled fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {d0, d1};
+    const cuuint64_t strides[1] = {stride_bytes};
+    const cuuint32_t box[2] = {b0, b1};
+    const cuuint32_t es[2] = {1, 1};
+    return fn(m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base),
+              dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 constexpr int TEX = 8, TEY = 8;
@@ -308,11 +422,56 @@ static size_t apply_smem() {
 
 constexpr int LTEX = 8, LTEY = 7, LNT = 256;
 
+template <class T> static CUtensorMap& wmap_ref(TmaCache& c);
+template <> CUtensorMap& wmap_ref<float>(TmaCache& c) { return c.w32; }
+template <> CUtensorMap& wmap_ref<double>(TmaCache& c) { return c.w64; }
+template <class T> static std::unordered_map<const void*, CUtensorMap>& umap_ref(TmaCache& c);
+template <> std::unordered_map<const void*, CUtensorMap>& umap_ref<float>(TmaCache& c) { return c.u32; }
+template <> std::unordered_map<const void*, CUtensorMap>& umap_ref<double>(TmaCache& c) { return c.u64; }
+
+template <class T>
+static const CUtensorMap& tma_wmap(TmaCache& c) { return wmap_ref<T>(c); }
+
+// Tensor map of a node vector (cached by address): the nx x ny grid, row pitch ld, box
+// UPT x (4*LTEY+5); coordinates outside the grid read as zero.
+template <class T>
+static const CUtensorMap* tma_umap(TmaCache& c, const T* x, const Layout& L) {
+    if (!c.ok) return nullptr;
+    auto& m = umap_ref<T>(c);
+    auto it = m.find(x);
+    if (it != m.end()) return &it->second;
+    if ((reinterpret_cast<uintptr_t>(x) & 15) != 0) return nullptr;
+    CUtensorMap tm;
+    if (!encode_2d(&tm, sizeof(T) == 8, x, (uint64_t)L.nx, (uint64_t)L.ny, (uint64_t)L.ld * sizeof(T), UPT,
+                   4 * LTEY + 5))
+        return nullptr;
+    return &(m[x] = tm);
+}
+
+// Encodes the element-data maps; leaves the cache disabled (plain loads) if TMA is unavailable.
+void tma_init(Handle& h) {
+    TmaCache& c = h.tma;
+    c.ok = false;
+    if (getenv("EQC_NO_TMA")) return;
+    const Layout& L = h.L;
+    const int EX = LTEX + 1, EY = LTEY + 1;
+    bool ok = encode_2d(&c.w32, false, h.W32p.p, (uint64_t)L.NelX * WPad<float>::v, (uint64_t)L.NelY,
+                        (uint64_t)L.NelX * WPad<float>::v * sizeof(float), EX * WPad<float>::v, EY);
+    ok = ok && encode_2d(&c.w64, true, h.W64p.p, (uint64_t)L.NelX * WPad<double>::v, (uint64_t)L.NelY,
+                         (uint64_t)L.NelX * WPad<double>::v * sizeof(double), EX * WPad<double>::v, EY);
+    c.ok = ok;
+}
+
 template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s) {
     if (mode <= 1) {
         dim3 grid(A.L.NelX / LTEX + 1, A.L.NelY / LTEY + 1);
-        k_apply_lines<T, LTEX, LTEY, LNT><<<grid, LNT, 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
+        const CUtensorMap* um = A.tma ? tma_umap<T>(*A.tma, x, A.L) : nullptr;
+        if (um) {
+            k_apply_tma<T, LTEX, LTEY, LNT><<<grid, LNT, 0, s>>>(*um, tma_wmap<T>(*A.tma), y, A, sign, mode == 1 ? 1 : 0);
+        } else {
+            k_apply_lines<T, LTEX, LTEY, LNT><<<grid, LNT, 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
+        }
         EQC_CHECK_LAUNCH();
         count_launch();
         return;

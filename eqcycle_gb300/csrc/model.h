@@ -23,7 +23,7 @@ struct Ctrl {
     long long it;
     double vhypo;          // max of 2v+Vpl over the fault and
     int ihypo;             // its first index
-    int pad;
+    int apply_err;         // set by the stiffness apply when a bounded TMA wait gives up
 };
 
 // Multigrid hierarchy (defined in mg.h).
@@ -42,8 +42,9 @@ struct Handle {
     std::vector<int64_t> ref2lay;    // [nglob] reference node (0-based) -> layout index
     DBuf<int64_t> d_ref2lay;
     // element data
-    DBuf<double> W64;
-    DBuf<float> W32;
+    DBuf<double> W64, W64p;
+    DBuf<float> W32, W32p;
+    TmaCache tma;
     double H[25];
     // node arrays [L.size()]
     DBuf<double> M, d, v, a, dPre, tmp64a, tmp64b;
@@ -93,8 +94,13 @@ void set_H(const double* H, cudaStream_t s);
 template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s);
 
-inline ApplyArgs<double> args64(const Handle& h) { return {h.W64.p, h.c1, h.c2, h.L}; }
-inline ApplyArgs<float> args32(const Handle& h) { return {h.W32.p, (float)h.c1, (float)h.c2, h.L}; }
+inline ApplyArgs<double> args64(Handle& h) {
+    return {h.W64.p, h.c1, h.c2, h.L, h.W64p.p, &h.ctrl.p->apply_err, &h.tma};
+}
+inline ApplyArgs<float> args32(Handle& h) {
+    return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma};
+}
+void tma_init(Handle& h);
 
 // blas.cu
 void dot64(Handle& h, const double* x, const double* y, int64_t n, double* out_dev);

@@ -228,6 +228,10 @@ static int pcg_mixed(Handle& h, double tol, int maxit, double* relres) {
 int qs_solve_device(Handle& h, double tol, int maxit, double* relres) {
     if (maxit <= 0) maxit = (int)std::min<int64_t>(h.L.size() - h.L.ld, 1 << 30);
     int it = (h.opt.precision == EQC_MIXED) ? pcg_mixed(h, tol, maxit, relres) : pcg_fp64(h, tol, maxit, relres);
+    int err = 0;
+    EQC_CUDA(cudaMemcpyAsync(&err, &h.ctrl.p->apply_err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    EQC_CUDA(cudaStreamSynchronize(h.stream));
+    if (err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
     h.cg_iters_total += it < 0 ? -it : it;
     h.qs_solves_total += 1;
     return it;

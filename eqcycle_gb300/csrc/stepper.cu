@@ -532,6 +532,7 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
         C.it = it_keep;
         if (C.fail != 0x7fffffff)
             throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(C.fail));
+        if (C.apply_err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
         const double Vfmax = C.Vfmax;
         if (!std::isfinite(Vfmax)) throw Error(EQC_E_NAN, "non-finite slip rate");
         // ---- outputs (main.jl:361-436) ----
