@@ -8,10 +8,14 @@
 namespace eqc {
 
 Handle::~Handle() {
+    destroy_graphs(*this);
     mg_destroy(*this);
     if (h_ctrl) cudaFreeHost(h_ctrl);
     if (h_scal) cudaFreeHost(h_scal);
-    if (stream) cudaStreamDestroy(stream);
+    if (h_cg) cudaFreeHost(h_cg);
+    for (cudaStream_t c : cap_streams)
+        if (c) cudaStreamDestroy(c);
+    if (own_stream) cudaStreamDestroy(own_stream);
 }
 
 static void fail_if(bool cond, const std::string& msg) {
@@ -48,7 +52,8 @@ static void create(Handle& h, const eqc_model& m) {
     fail_if(m.IDstate != 2, "only IDstate = 2 (aging law, log form) is on the hot path");
     fail_if(m.ETA != 0.0, "Kelvin-Voigt damping (ETA != 0) is not on the hot path");
     EQC_CUDA(cudaSetDevice(h.opt.device));
-    EQC_CUDA(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+    EQC_CUDA(cudaStreamCreateWithFlags(&h.own_stream, cudaStreamNonBlocking));
+    h.stream = h.own_stream;
     cudaStream_t s = h.stream;
     Layout& L = h.L;
     L.NelX = (int)m.NelX;
@@ -117,7 +122,8 @@ static void create(Handle& h, const eqc_model& m) {
     const int64_t N = L.size();
     std::vector<double> Mlay(N, 1.0);
     for (int64_t g = 0; g < m.nglob; ++g) Mlay[h.ref2lay[g]] = m.M[g];
-    for (DBuf<double>* b : {&h.M, &h.d, &h.v, &h.a, &h.dPre, &h.tmp64a, &h.tmp64b, &h.r64, &h.z64, &h.p64, &h.q64})
+    for (DBuf<double>* b : {&h.M, &h.d, &h.v, &h.a, &h.dPre, &h.tmp64a, &h.tmp64b, &h.tmp64c, &h.r64, &h.z64, &h.p64,
+                             &h.q64})
         b->alloc(N);
     for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32}) b->alloc(N);
     h.M.upload(Mlay.data(), N, s);
@@ -176,7 +182,7 @@ static void create(Handle& h, const eqc_model& m) {
     F.NFBC0 = nfbc;
     for (DBuf<double>* b : {&F.fo, &F.Vo, &F.xLf, &F.cca, &F.ccb, &F.Seff, &F.tauo, &F.XiLf, &F.FltB, &F.FltZ, &F.FltX,
                             &F.Mf, &F.psi, &F.psi1, &F.psi2, &F.tau, &F.tau1, &F.tau2, &F.Vf, &F.Vf0, &F.Vf1, &F.Vf2,
-                            &F.FltVfree, &F.vPre})
+                            &F.FltVfree, &F.vPre, &F.Flast})
         b->alloc(Nf);
     F.fo.upload(m.fo, Nf, s);
     F.Vo.upload(m.Vo, Nf, s);
@@ -209,6 +215,9 @@ static void create(Handle& h, const eqc_model& m) {
     h.red_count.alloc(64);
     h.scal.alloc(16);
     EQC_CUDA(cudaMallocHost(&h.h_scal, sizeof(double) * 16));
+    h.cg.alloc(1);
+    EQC_CUDA(cudaMallocHost(&h.h_cg, sizeof(CGState)));
+    std::memset(h.h_cg, 0, sizeof(CGState));
     EQC_CUDA(cudaStreamSynchronize(s));
     if (h.opt.precond == EQC_PC_AMG) mg_build(h);
 }
@@ -401,6 +410,7 @@ eqc_status eqc_set_state(eqc_handle* H, const char* name, const double* in) {
             to_layout(h, in, l);
             b->upload(l.data(), l.size(), h.stream);
         }
+        invalidate_residual(h);
         EQC_CUDA(cudaStreamSynchronize(h.stream));
     });
 }
@@ -415,8 +425,13 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         else if (s == "dt") *out = C.dt;
         else if (s == "isolver") *out = C.isolver;
         else if (s == "it") *out = (double)C.it;
-        else if (s == "cg_iters") *out = (double)h.cg_iters_total;
-        else if (s == "qs_solves") *out = (double)h.qs_solves_total;
+        else if (s == "cg_iters" || s == "qs_solves" || s == "cg_updates" || s == "cg_carried") {
+            Ctrl c;
+            EQC_CUDA(cudaMemcpyAsync(&c, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h.stream));
+            EQC_CUDA(cudaStreamSynchronize(h.stream));
+            *out = (double)(s == "cg_iters" ? c.cg_iters : s == "qs_solves" ? c.cg_solves
+                            : s == "cg_updates" ? c.cg_updates : c.cg_carried);
+        }
         else throw Error(EQC_E_ARG, "unknown scalar " + s);
     });
 }
@@ -436,6 +451,7 @@ eqc_status eqc_set_scalar(eqc_handle* H, const char* name, double value) {
             if (value != 1 && value != 2) throw Error(EQC_E_ARG, "isolver must be 1 or 2");
             C.isolver = (int)value;
         } else throw Error(EQC_E_ARG, "unknown or read-only scalar " + s);
+        C.r_valid = 0;
         EQC_CUDA(cudaMemcpyAsync(h.ctrl.p, h.h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, h.stream));
         EQC_CUDA(cudaStreamSynchronize(h.stream));
     });

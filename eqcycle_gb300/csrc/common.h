@@ -116,8 +116,10 @@ struct ApplyArgs {
 // Error text for entry points without a handle (returned by eqc_last_error(NULL)).
 void set_thread_error(const std::string& msg);
 
-// Kernel counters (what the library launched).
+// Kernel counters (what the library launched).  While a graph is being captured the
+// count goes to a capture tally instead; graph launches add what they execute.
 extern int64_t g_launches;
-inline void count_launch(int n = 1) { g_launches += n; }
+extern thread_local int64_t* g_count_target;
+inline void count_launch(int n = 1) { *(g_count_target ? g_count_target : &g_launches) += n; }
 
 }  // namespace eqc

@@ -25,13 +25,6 @@ template <class T> __device__ __forceinline__ T Hc(int i, int j);
 template <> __device__ __forceinline__ double Hc<double>(int i, int j) { return cH64[i + 5 * j]; }
 template <> __device__ __forceinline__ float Hc<float>(int i, int j) { return cH32[i + 5 * j]; }
 
-void set_H(const double* H, cudaStream_t s) {
-    float hf[25];
-    for (int k = 0; k < 25; ++k) hf[k] = (float)H[k];
-    EQC_CUDA(cudaMemcpyToSymbolAsync(cH64, H, sizeof(double) * 25, 0, cudaMemcpyHostToDevice, s));
-    EQC_CUDA(cudaMemcpyToSymbolAsync(cH32, hf, sizeof(float) * 25, 0, cudaMemcpyHostToDevice, s));
-    EQC_CUDA(cudaStreamSynchronize(s));
-}
 
 // mode 0: full apply, every owned node written
 // mode 1: full apply, fault row (iy = 0) written as zero (interior operator K_II)
@@ -462,6 +455,19 @@ void tma_init(Handle& h) {
     c.ok = ok;
 }
 
+void set_H(const double* H, cudaStream_t s) {
+    float hf[25];
+    for (int k = 0; k < 25; ++k) hf[k] = (float)H[k];
+    EQC_CUDA(cudaMemcpyToSymbolAsync(cH64, H, sizeof(double) * 25, 0, cudaMemcpyHostToDevice, s));
+    EQC_CUDA(cudaMemcpyToSymbolAsync(cH32, hf, sizeof(float) * 25, 0, cudaMemcpyHostToDevice, s));
+    EQC_CUDA(cudaStreamSynchronize(s));
+    // kernel attributes are set here, at handle creation, never during a stream capture
+    EQC_CUDA(cudaFuncSetAttribute(k_apply<double, TEX, TEY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)apply_smem<double>()));
+    EQC_CUDA(cudaFuncSetAttribute(k_apply<float, TEX, TEY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)apply_smem<float>()));
+}
+
 template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s) {
     if (mode <= 1) {
@@ -476,12 +482,7 @@ void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStre
         count_launch();
         return;
     }
-    static bool attr_set = false;
     const size_t sm = apply_smem<T>();
-    if (!attr_set) {
-        EQC_CUDA(cudaFuncSetAttribute(k_apply<T, TEX, TEY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr_set = true;
-    }
     dim3 grid((A.L.NelX + TEX - 1) / TEX, mode >= 2 ? 1 : (A.L.NelY + TEY - 1) / TEY);
     k_apply<T, TEX, TEY><<<grid, 256, sm, s>>>(x, y, A, sign, mode);
     EQC_CHECK_LAUNCH();

@@ -72,6 +72,62 @@ __global__ void k_restrict(const T* __restrict__ rf, T* __restrict__ bc, int ncx
     }
 }
 
+// ---- transfers between the spectral-element grid and the element-vertex grid ----------
+// The GLL node at local index k of an element interpolates the element's two vertices with
+// weights lo[k] (lower vertex) and hi[k] (upper vertex), k = 0..3; the last node of the
+// lattice is the last vertex.  Structured: no index tables, no integer division.
+template <class T>
+struct GllW {
+    T lo[4], hi[4];
+};
+
+// xf[iy, 4ex + k] += P0 xc  for node rows iy >= 1; one thread per (element column, node row),
+// the thread of the last element column also takes the lattice's last node.
+template <class T>
+__global__ void k_prolong_sem(const T* __restrict__ xc, T* __restrict__ xf, Layout L, int ldc, GllW<T> w) {
+    const int ex = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iy = blockIdx.y + 1;
+    if (ex >= L.NelX || iy >= L.ny) return;
+    const int ey = min(iy >> 2, L.NelY - 1), ky = iy - 4 * ey;
+    const T wyl = ky == 4 ? T(0) : w.lo[ky], wyh = ky == 4 ? T(1) : w.hi[ky];
+    const T* c0 = xc + (int64_t)ey * ldc + ex;
+    const T* c1 = c0 + ldc;
+    const T a0 = wyl * c0[0] + wyh * c1[0];       // vertex column ex
+    const T a1 = wyl * c0[1] + wyh * c1[1];       // vertex column ex + 1
+    T* row = xf + (int64_t)iy * L.ld + 4 * ex;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) row[k] += w.lo[k] * a0 + w.hi[k] * a1;
+    if (ex == L.NelX - 1) row[4] += a1;
+}
+
+// bc[vy, vx] = (P0^T rf)[vy, vx] over fine rows iy >= 1; coarse row 0 = 0.  One thread per vertex.
+template <class T>
+__global__ void k_restrict_sem(const T* __restrict__ rf, T* __restrict__ bc, Layout L, int ldc, GllW<T> w) {
+    const int vx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int vy = blockIdx.y;
+    const int ncx = L.NelX + 1;
+    if (vx >= ncx) return;
+    T acc = T(0);
+    if (vy >= 1) {
+        for (int dy = -3; dy <= 3; ++dy) {
+            const int iy = 4 * vy + dy;
+            if (iy < 1 || iy >= L.ny) continue;
+            const T wy = dy == 0 ? T(1) : (dy > 0 ? (vy < L.NelY ? w.lo[dy] : T(0)) : w.hi[4 + dy]);
+            const T* row = rf + (int64_t)iy * L.ld;
+            T sx = T(0);
+#pragma unroll
+            for (int dx = -3; dx <= 3; ++dx) {
+                const int ix = 4 * vx + dx;
+                if (ix < 0 || ix >= L.nx) continue;
+                const T wx = dx == 0 ? T(1) : (dx > 0 ? (vx < L.NelX ? w.lo[dx] : T(0)) : w.hi[4 + dx]);
+                sx += wx * row[ix];
+            }
+            acc += wy * sx;
+        }
+    }
+    bc[(int64_t)vy * ldc + vx] = acc;
+}
+
 // Chebyshev, first step.  with_x: r = Dinv (b - t) with t = A x ; else r = Dinv b, x = 0.
 // d = r/theta ; x += d
 template <class T>
@@ -161,6 +217,16 @@ template <> struct Sel<float> {
     static ApplyArgs<float> args(Handle& h) { return args32(h); }
 };
 
+template <class T>
+static GllW<T> gll_weights(const MGHier& m) {
+    GllW<T> g;
+    for (int k = 0; k < 4; ++k) {
+        g.lo[k] = (T)m.gll_lo[k];
+        g.hi[k] = (T)m.gll_hi[k];
+    }
+    return g;
+}
+
 // y = A_l x on level l (0 = spectral-element grid)
 template <class T>
 static void level_apply(Handle& h, int l, const T* x, T* y) {
@@ -234,13 +300,23 @@ static void vcycle(Handle& h, int l, T* x, const T* b) {
     MGWork& wc = m.work[l + 1];
     T* bc = Sel<T>::b(wc);
     T* xc = Sel<T>::x(wc);
-    k_restrict<T><<<vb((int64_t)tr.ncx * tr.ncy), 256, 0, h.stream>>>(r, bc, tr.ncx, tr.ncy, tr.ldf, tr.ldc, tr.rpx.p,
-                                                                       tr.rix.p, Sel<T>::rwx(tr), tr.rpy.p, tr.riy.p,
-                                                                       Sel<T>::rwy(tr));
+    const GllW<T> gw = gll_weights<T>(m);
+    if (l == 0) {
+        k_restrict_sem<T><<<dim3((tr.ncx + 127) / 128, tr.ncy), 128, 0, h.stream>>>(r, bc, h.L, tr.ldc, gw);
+    } else {
+        k_restrict<T><<<vb((int64_t)tr.ncx * tr.ncy), 256, 0, h.stream>>>(r, bc, tr.ncx, tr.ncy, tr.ldf, tr.ldc,
+                                                                           tr.rpx.p, tr.rix.p, Sel<T>::rwx(tr), tr.rpy.p,
+                                                                           tr.riy.p, Sel<T>::rwy(tr));
+    }
     count_launch();
     vcycle<T>(h, l + 1, xc, bc);
-    k_prolong_add<T><<<vb((int64_t)tr.nfx * tr.nfy), 256, 0, h.stream>>>(xc, x, tr.nfx, tr.nfy, tr.ldf, tr.ldc, tr.px.p,
-                                                                         tr.py.p, Sel<T>::wx(tr), Sel<T>::wy(tr));
+    if (l == 0) {
+        k_prolong_sem<T><<<dim3((h.L.NelX + 127) / 128, h.L.ny - 1), 128, 0, h.stream>>>(xc, x, h.L, tr.ldc, gw);
+    } else {
+        k_prolong_add<T><<<vb((int64_t)tr.nfx * tr.nfy), 256, 0, h.stream>>>(xc, x, tr.nfx, tr.nfy, tr.ldf, tr.ldc,
+                                                                             tr.px.p, tr.py.p, Sel<T>::wx(tr),
+                                                                             Sel<T>::wy(tr));
+    }
     count_launch();
     EQC_CHECK_LAUNCH();
     chebyshev<T>(h, l, x, b, true);
@@ -352,13 +428,20 @@ void mg_build(Handle& h) {
     std::vector<Transfer1D> tx, ty;
     tx.push_back(make_gll_transfer(L.NelX, xg));
     ty.push_back(make_gll_transfer(L.NelY, xg));
+    for (int k = 0; k < 4; ++k) {   // weights of local node k (identical in every element)
+        m.gll_lo[k] = tx[0].p_w[2 * k];
+        m.gll_hi[k] = tx[0].p_w[2 * k + 1];
+    }
     StencilLevel l1;
     l1.cx = L.NelX + 1;
     l1.cy = L.NelY + 1;
     l1.A = vertex_operator(h, Wh.data());
     m.lev.push_back(std::move(l1));
     // coarser vertex grids
-    while ((int64_t)m.lev.back().cx * (m.lev.back().cy - 1) > 1024 && m.lev.back().cx >= 5 && m.lev.back().cy >= 5) {
+    const int64_t coarse_max = h.opt.mg_coarse_max > 0 ? h.opt.mg_coarse_max : 2048;
+    if (h.opt.mg_degree > 0) m.deg = h.opt.mg_degree;
+    while ((int64_t)m.lev.back().cx * (m.lev.back().cy - 1) > coarse_max && m.lev.back().cx >= 5 &&
+           m.lev.back().cy >= 5) {
         StencilLevel& f = m.lev.back();
         Transfer1D ax = make_coarsen_transfer(f.cx), ay = make_coarsen_transfer(f.cy);
         StencilLevel c;

@@ -51,9 +51,10 @@ struct MGWork {                  // per-level vectors, full layout of the level
 };
 
 struct MGHier {
-    int deg = 3;
+    int deg = 4;
     double lo_ratio = 30.0;
     double lmax0 = 0;
+    double gll_lo[4] = {0, 0, 0, 0}, gll_hi[4] = {0, 0, 0, 0};   // SEM <-> vertex weights
     DBuf<double> Dinv0_64;
     DBuf<float> Dinv0_32;
     std::vector<StencilLevel> lev;    // levels 1..L

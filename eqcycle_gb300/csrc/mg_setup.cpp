@@ -202,16 +202,19 @@ std::vector<double> dense_inverse_spd(const std::vector<double>& A9, int cx, int
             const double s = 0.5 * (M[(size_t)i * n + j] + M[(size_t)j * n + i]);
             M[(size_t)i * n + j] = M[(size_t)j * n + i] = s;
         }
-    std::vector<double> Lm(M);
+    // banded Cholesky M = L L^T: with rows numbered lexicographically the 9-point stencil
+    // couples rows at most cx + 1 apart, and L keeps that bandwidth
+    const int bw = std::min(n - 1, cx + 1);
+    std::vector<double> Lm((size_t)n * n, 0.0);
     for (int j = 0; j < n; ++j) {
-        double d = Lm[(size_t)j * n + j];
-        for (int k = 0; k < j; ++k) d -= Lm[(size_t)j * n + k] * Lm[(size_t)j * n + k];
+        double d = M[(size_t)j * n + j];
+        for (int k = std::max(0, j - bw); k < j; ++k) d -= Lm[(size_t)j * n + k] * Lm[(size_t)j * n + k];
         if (!(d > 0)) throw Error(EQC_E_ARG, "coarsest multigrid operator is not positive definite");
         d = std::sqrt(d);
         Lm[(size_t)j * n + j] = d;
-        for (int i = j + 1; i < n; ++i) {
-            double s = Lm[(size_t)i * n + j];
-            for (int k = 0; k < j; ++k) s -= Lm[(size_t)i * n + k] * Lm[(size_t)j * n + k];
+        for (int i = j + 1; i <= std::min(n - 1, j + bw); ++i) {
+            double s = M[(size_t)i * n + j];
+            for (int k = std::max(0, i - bw); k < j; ++k) s -= Lm[(size_t)i * n + k] * Lm[(size_t)j * n + k];
             Lm[(size_t)i * n + j] = s / d;
         }
     }
@@ -219,14 +222,14 @@ std::vector<double> dense_inverse_spd(const std::vector<double>& A9, int cx, int
     for (int c = 0; c < n; ++c) {
         std::fill(col.begin(), col.end(), 0.0);
         col[c] = 1.0;
-        for (int i = 0; i < n; ++i) {  // L y = e_c
+        for (int i = c; i < n; ++i) {  // L y = e_c (y = 0 above row c)
             double s = col[i];
-            for (int k = 0; k < i; ++k) s -= Lm[(size_t)i * n + k] * col[k];
+            for (int k = std::max(c, i - bw); k < i; ++k) s -= Lm[(size_t)i * n + k] * col[k];
             col[i] = s / Lm[(size_t)i * n + i];
         }
         for (int i = n - 1; i >= 0; --i) {  // L^T x = y
             double s = col[i];
-            for (int k = i + 1; k < n; ++k) s -= Lm[(size_t)k * n + i] * col[k];
+            for (int k = i + 1; k <= std::min(n - 1, i + bw); ++k) s -= Lm[(size_t)k * n + i] * col[k];
             col[i] = s / Lm[(size_t)i * n + i];
         }
         for (int i = 0; i < n; ++i) Inv[(size_t)i * n + c] = col[i];

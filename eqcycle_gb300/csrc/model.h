@@ -11,6 +11,7 @@ struct FaultDev {
     int NFBC0 = 0;  // first friction node (0-based), NFBC - 1 of src/main.jl:186
     DBuf<double> fo, Vo, xLf, cca, ccb, Seff, tauo, XiLf, FltB, FltZ, FltX, Mf;
     DBuf<double> psi, psi1, psi2, tau, tau1, tau2, Vf, Vf0, Vf1, Vf2, FltVfree, vPre;
+    DBuf<double> Flast;   // fault displacement the carried CG residual belongs to
     DBuf<int> creep;   // 1 for fault nodes listed in iFBC (creeping), [Nf]
 };
 
@@ -24,6 +25,37 @@ struct Ctrl {
     double vhypo;          // max of 2v+Vpl over the fault and
     int ihypo;             // its first index
     int apply_err;         // set by the stiffness apply when a bounded TMA wait gives up
+    // quasi-static solve counters, accumulated on the device
+    long long cg_iters;    // CG iterations over all solves
+    long long cg_solves;   // solves
+    long long cg_updates;  // reliable updates (mixed precision)
+    long long cg_carried;  // solves that started from the carried residual
+    int cg_fail;           // bit 0: a solve reached maxit; bit 1: non-finite residual
+    int cg_last_it;        // iterations of the last solve
+    double cg_last_relres; // ||r|| / ||b|| of the last solve
+    int r_valid;           // r64 holds the FP64 true residual of d with fault row Flast
+                           // (mixed precision: carried into the next solve)
+};
+
+// Device-resident scalars of one CG solve.
+struct CGState {
+    double rho, rho_prev, pq, rr, bb;
+    double nb, reltol, res, rmax;
+    int it, maxit;
+    int done;          // 0 running, 1 converged, 2 maxit reached, 3 non-finite residual
+    int need_update;   // mixed precision: a reliable update is due
+};
+
+// A captured time step (one per regime) and the kernels it launches.
+struct StepGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t k_fixed = 0;     // kernels outside conditional bodies
+    int64_t k_iter = 0;      // kernels of one CG iteration (while body, without the update)
+    int64_t k_update = 0;    // kernels of one reliable update (if body)
+    int64_t k_carry = 0;     // kernels of a carried residual set-up (if body)
+    int64_t k_full = 0;      // kernels of a full residual set-up (if body)
+    int64_t k_bodies = 0;    // capture tally of all conditional bodies
 };
 
 // Multigrid hierarchy (defined in mg.h).
@@ -32,7 +64,14 @@ struct MGHier;
 struct Handle {
     eqc_options opt{};
     std::string err;
+    // Stream that work is enqueued on: the handle's own stream, or, while a conditional
+    // body of a step graph is being captured, that body's capture stream.
     cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t cap_streams[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaStream_t> stream_stack;
+    StepGraph graphs[2];       // [0] quasi-static step, [1] dynamic step
+    StepGraph* capturing = nullptr;   // graph whose capture is in progress
     int device = 0;
     Layout L{};
     int64_t nglob = 0, Nel = 0;
@@ -47,7 +86,7 @@ struct Handle {
     TmaCache tma;
     double H[25];
     // node arrays [L.size()]
-    DBuf<double> M, d, v, a, dPre, tmp64a, tmp64b;
+    DBuf<double> M, d, v, a, dPre, tmp64a, tmp64b, tmp64c;
     DBuf<double> diag64;   // diagonal of K (rows >= 1), Jacobi preconditioner
     DBuf<float> diag32;
     // boundary lists (layout indices) and coefficients
@@ -64,8 +103,10 @@ struct Handle {
     // reductions
     DBuf<double> red_part;        // partial sums
     DBuf<unsigned int> red_count; // last-block counters
-    DBuf<double> scal;            // CG scalars
+    DBuf<double> scal;            // scratch scalars (power iterations, timing)
     double* h_scal = nullptr;     // pinned mirror
+    DBuf<CGState> cg;             // CG scalars
+    CGState* h_cg = nullptr;      // pinned mirror
     // CG work vectors
     DBuf<double> r64, z64, p64, q64;
     DBuf<float> r32, z32, p32, q32, x32;
@@ -84,8 +125,6 @@ struct Handle {
     double tvsx = 0, tvsxinc = 0, tevneinc = 0.5, tevneb = 0, tevne = 0;
     int64_t idelevne = 0, ntvsx = 0, nevne = 0, slipstart = 0, idd = 0, it_s = 0, it_e = 0, rit = 0;
     std::vector<double> delfref;
-    // statistics
-    int64_t cg_iters_total = 0, qs_solves_total = 0;
     ~Handle();
 };
 
@@ -107,10 +146,32 @@ void dot64(Handle& h, const double* x, const double* y, int64_t n, double* out_d
 void dot32(Handle& h, const float* x, const float* y, int64_t n, double* out_dev);
 
 // solver.cu
+// Enqueues one CG solve on h.stream.  graph: inside a stream capture, the iteration loop
+// becomes a conditional while node; otherwise the host drives it (one sync per iteration).
+// carry: mixed precision in the time loop may start from the residual the previous solve
+// left (r_valid), updated for the change of the fault row, instead of a full FP64 apply.
+void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry = false);
+// Marks the carried residual stale (after the state was changed from outside the loop).
+void invalidate_residual(Handle& h);
 int qs_solve_device(Handle& h, double tol, int maxit, double* relres);
+
+// graph.cu
+// Handle of a conditional node of the graph h.stream is capturing (value 0 at each launch
+// unless a kernel upstream of the node sets it).
+cudaGraphConditionalHandle cond_handle(Handle& h);
+// Conditional node with handle c on the stream h.stream is capturing; until cond_end,
+// h.stream is the capture stream of the node's body.
+void cond_begin(Handle& h, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle c);
+void cond_end(Handle& h);
+// Ends every capture in progress on the handle's streams and restores h.stream.
+void abort_capture(Handle& h);
+// Kernel counting during capture (count_launch adds to the capture tally instead).
+void capture_counting(bool on);
+int64_t capture_tally();
 
 // stepper.cu
 void init_state(Handle& h, double V_init);
+void destroy_graphs(Handle& h);
 void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st);
 void fault_slrFunc(Handle& h, const double* psi, double* psi1, const double* Vf, double* Vf1, const double* tau1,
                    double dt);

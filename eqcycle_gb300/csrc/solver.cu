@@ -15,21 +15,36 @@
 // Convergence is always certified on an FP64 true residual.
 #include "model.h"
 #include "reduce.cuh"
+#include "vec.cuh"
 #include <cmath>
+#include <cstddef>
 
 namespace eqc {
 
-enum { S_RHO = 0, S_RHOP = 1, S_PQ = 2, S_RR = 3, S_BB = 4, S_R0 = 5, S_NSLOT = 16 };
+// Slots of the scalar block the vector kernels address (the leading doubles of CGState).
+enum { S_RHO = 0, S_RHOP = 1, S_PQ = 2, S_RR = 3, S_BB = 4 };
+static_assert(offsetof(CGState, rho_prev) == 8 * S_RHOP && offsetof(CGState, pq) == 8 * S_PQ &&
+                  offsetof(CGState, rr) == 8 * S_RR && offsetof(CGState, bb) == 8 * S_BB,
+              "CGState must start with rho, rho_prev, pq, rr, bb");
+
+// The vector kernels run on a fixed grid of VEC_BLOCKS x VEC_THREADS threads over 4-wide
+// chunks (n is a multiple of 4: every vector is a whole number of 8-entry-aligned rows);
+// reductions are deterministic (fixed slices, partials summed in CTA order).
 
 // dot into S_RHO, shifting the previous value into S_RHOP
 template <class T>
-__global__ void __launch_bounds__(RED_THREADS) k_dot_rho(const T* __restrict__ x, const T* __restrict__ y, int64_t n,
+__global__ void __launch_bounds__(VEC_THREADS) k_dot_rho(const T* __restrict__ x, const T* __restrict__ y, int64_t n,
                                                          double* part, unsigned* count, double* S) {
     __shared__ double sh[32];
-    double s = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        s += (double)x[i] * (double)y[i];
-    s = block_sum(s, sh);
+    DotAcc<T> acc;
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        T a[4], b[4];
+        ld4(x + i, a);
+        ld4(y + i, b);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc.add(a[k], b[k]);
+    }
+    const double s = block_sum(acc.value(), sh);
     finish_reduction(s, part, count, sh, [&](double t) {
         S[S_RHOP] = S[S_RHO];
         S[S_RHO] = t;
@@ -38,29 +53,46 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot_rho(const T* __restrict__ x
 
 // u = z + (rho / rho_prev) u
 template <class T>
-__global__ void k_pupdate(const T* __restrict__ z, T* __restrict__ u, int64_t n, const double* S) {
-    const double beta = S[S_RHO] / S[S_RHOP];
-    const T b = (T)beta;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        u[i] = z[i] + b * u[i];
+__global__ void __launch_bounds__(VEC_THREADS) k_pupdate(const T* __restrict__ z, T* __restrict__ u, int64_t n,
+                                                         const double* S) {
+    const T b = (T)(S[S_RHO] / S[S_RHOP]);
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        T zz[4], uu[4];
+        ld4(z + i, zz);
+        ld4(u + i, uu);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) uu[k] = zz[k] + b * uu[k];
+        st4(u + i, uu);
+    }
 }
 
 // x += alpha u ; r -= alpha q ; S_RR = r.r   (alpha = rho / (u.q))
 template <class TX, class T>
-__global__ void __launch_bounds__(RED_THREADS) k_xr_update(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ u,
+__global__ void __launch_bounds__(VEC_THREADS) k_xr_update(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ u,
                                                            const T* __restrict__ q, int64_t n, double* part,
                                                            unsigned* count, double* S) {
     __shared__ double sh[32];
     const double alpha = S[S_RHO] / S[S_PQ];
     const T a = (T)alpha;
-    double s = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] = x[i] + (TX)alpha * (TX)u[i];
-        const T ri = r[i] - a * q[i];
-        r[i] = ri;
-        s += (double)ri * (double)ri;
+    const TX ax = (TX)alpha;
+    DotAcc<T> acc;
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        TX xx[4];
+        T rr[4], uu[4], qq[4];
+        ld4(x + i, xx);
+        ld4(r + i, rr);
+        ld4(u + i, uu);
+        ld4(q + i, qq);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            xx[k] = xx[k] + ax * (TX)uu[k];
+            rr[k] = rr[k] - a * qq[k];
+            acc.add(rr[k], rr[k]);
+        }
+        st4(x + i, xx);
+        st4(r + i, rr);
     }
-    s = block_sum(s, sh);
+    const double s = block_sum(acc.value(), sh);
     finish_reduction(s, part, count, sh, [&](double t) { S[S_RR] = t; });
 }
 
@@ -70,34 +102,161 @@ __global__ void k_jacobi(const T* __restrict__ r, const T* __restrict__ dg, T* _
         z[i] = r[i] / dg[i];
 }
 
-__global__ void k_set_scalar(double* S, int slot, double v) { S[slot] = v; }
-
 // x64 += (double) y32 ; y32 = 0
-__global__ void k_fold(double* __restrict__ x, float* __restrict__ y, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] += (double)y[i];
-        y[i] = 0.f;
+__global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, float* __restrict__ y, int64_t n) {
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        double xx[4];
+        float yy[4];
+        ld4(x + i, xx);
+        ld4(y + i, yy);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) xx[k] += (double)yy[k];
+        st4(x + i, xx);
+        const float zero[4] = {0.f, 0.f, 0.f, 0.f};
+        st4(y + i, zero);
     }
 }
 // r32 = (float) r64 ; S_RR = r64.r64
-__global__ void __launch_bounds__(RED_THREADS) k_demote_norm(const double* __restrict__ r64, float* __restrict__ r32,
+__global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(const double* __restrict__ r64, float* __restrict__ r32,
                                                              int64_t n, double* part, unsigned* count, double* S) {
     __shared__ double sh[32];
     double s = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v = r64[i];
-        r32[i] = (float)v;
-        s += v * v;
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        double v[4];
+        float f[4];
+        ld4(r64 + i, v);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            f[k] = (float)v[k];
+            s += v[k] * v[k];
+        }
+        st4(r32 + i, f);
     }
     s = block_sum(s, sh);
     finish_reduction(s, part, count, sh, [&](double t) { S[S_RR] = t; });
 }
 
-static inline dim3 vgrid() { return dim3(RED_BLOCKS); }
+static inline dim3 vgrid() { return dim3(VEC_BLOCKS); }
 
-static void read_scalars(Handle& h) {
-    EQC_CUDA(cudaMemcpyAsync(h.h_scal, h.scal.p, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, h.stream));
+// ---- device-side control of the CG loop -----------------------------------------------
+// Every control kernel is a single thread: it owns the CGState and is the only caller of
+// cudaGraphSetConditional for its node (concurrent calls on one handle are undefined).
+
+// Start of a solve: S->bb, S->rr hold ||b||^2 and ||r0||^2.
+__global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, cudaGraphConditionalHandle hw, int use_cond) {
+    const double nb = sqrt(S->bb), r = sqrt(S->rr);
+    const double reltol = (rule == EQC_TOL_R0 ? r : nb) * tol;
+    S->nb = nb;
+    S->reltol = reltol;
+    S->res = r;
+    S->rmax = r;
+    S->it = 0;
+    S->maxit = maxit;
+    S->rho = 1.0;
+    S->rho_prev = 1.0;
+    S->need_update = 0;
+    const int st = !isfinite(r) ? 3 : (r <= reltol ? 1 : (maxit <= 0 ? 2 : 0));
+    S->done = st;
+    if (use_cond) cudaGraphSetConditional(hw, st == 0 ? 1u : 0u);
+}
+
+// End of an FP64 iteration: the loop goes on until ||r|| <= reltol or maxit.
+__global__ void k_cg_check(CGState* S, cudaGraphConditionalHandle hw, int use_cond) {
+    S->it += 1;
+    const double r = sqrt(S->rr);
+    S->res = r;
+    const int st = !isfinite(r) ? 3 : (r <= S->reltol ? 1 : (S->it >= S->maxit ? 2 : 0));
+    S->done = st;
+    if (use_cond) cudaGraphSetConditional(hw, st == 0 ? 1u : 0u);
+}
+
+// Mixed precision, after the FP32 recurrences: decide whether a reliable update is due
+// (the recurrence residual fell by `delta` since the last one, or the loop would stop).
+__global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandle hi, int use_cond) {
+    S->it += 1;
+    const double rs = sqrt(S->rr);
+    int need = 0;
+    if (!isfinite(rs)) {
+        S->done = 3;
+    } else {
+        S->rmax = fmax(S->rmax, rs);
+        need = (rs < delta * S->rmax || rs <= S->reltol || S->it >= S->maxit) ? 1 : 0;
+    }
+    S->res = rs;
+    S->need_update = need;
+    if (use_cond) cudaGraphSetConditional(hi, need ? 1u : 0u);
+}
+
+// Mixed precision, end of the iteration: take the FP64 residual of a reliable update and
+// decide whether the loop goes on.
+__global__ void k_cg_check_b(CGState* S, Ctrl* C, cudaGraphConditionalHandle hw, int use_cond) {
+    if (S->done != 3) {
+        if (S->need_update) {
+            const double rs = sqrt(S->rr);
+            S->res = rs;
+            S->rmax = rs;
+            S->need_update = 0;
+            C->cg_updates += 1;
+        }
+        const double r = S->res;
+        S->done = !isfinite(r) ? 3 : (r <= S->reltol ? 1 : (S->it >= S->maxit ? 2 : 0));
+    }
+    if (use_cond) cudaGraphSetConditional(hw, S->done == 0 ? 1u : 0u);
+}
+
+// After the loop: solve counters and failure flags in the control block.  mark_valid: the
+// loop ended on an FP64 true residual (mixed precision), which the next solve may carry.
+__global__ void k_cg_finish(const CGState* S, Ctrl* C, int mark_valid) {
+    C->r_valid = (mark_valid && S->done == 1) ? 1 : 0;
+    C->cg_iters += S->it;
+    C->cg_solves += 1;
+    C->cg_last_it = S->it;
+    C->cg_last_relres = S->nb > 0 ? S->res / S->nb : S->res;
+    if (S->done == 2) C->cg_fail |= 1;
+    if (S->done == 3) C->cg_fail |= 2;
+}
+
+// Fault row: dF = d[k] - Flast[k] into row 0 of a work vector, Flast = d[k].
+__global__ void k_fault_delta(const double* __restrict__ d, double* __restrict__ Flast, double* __restrict__ dF,
+                              int Nf) {
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < Nf; k += blockDim.x * gridDim.x) {
+        const double f = d[k];
+        dF[k] = f - Flast[k];
+        Flast[k] = f;
+    }
+}
+
+// Carried residual, rows 1..4 (the only rows K_IF reaches): r64 += t, r32 = (float) r64,
+// S_RR += sum(r_new^2 - r_old^2).
+__global__ void __launch_bounds__(VEC_THREADS) k_carry_rows(double* __restrict__ r64, float* __restrict__ r32,
+                                                            const double* __restrict__ t, int64_t n, double* part,
+                                                            unsigned* count, double* S) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double ro = r64[i], rn = ro + t[i];
+        r64[i] = rn;
+        r32[i] = (float)rn;
+        s += rn * rn - ro * ro;
+    }
+    s = block_sum(s, sh);
+    finish_reduction(s, part, count, sh, [&](double tt) { S[S_RR] += tt; });
+}
+
+// Chooses the residual set-up of a solve: carry (r_valid) or a full FP64 apply.
+__global__ void k_setup_select(Ctrl* C, cudaGraphConditionalHandle hc, cudaGraphConditionalHandle hf, int use_cond) {
+    const unsigned v = C->r_valid ? 1u : 0u;
+    C->cg_carried += v;
+    if (use_cond) {
+        cudaGraphSetConditional(hc, v);
+        cudaGraphSetConditional(hf, 1u - v);
+    }
+}
+
+static const CGState& read_cg(Handle& h) {
+    EQC_CUDA(cudaMemcpyAsync(h.h_cg, h.cg.p, sizeof(CGState), cudaMemcpyDeviceToHost, h.stream));
     EQC_CUDA(cudaStreamSynchronize(h.stream));
+    return *h.h_cg;
 }
 
 template <class T>
@@ -108,7 +267,7 @@ void precond<double>(Handle& h, const double* r, double* z, int64_t n) {
     if (h.opt.precond == EQC_PC_AMG) {
         mg_apply64(h, r, z);
     } else {
-        k_jacobi<double><<<vgrid(), RED_THREADS, 0, h.stream>>>(r, h.diag64.p + h.L.ld, z, n);
+        k_jacobi<double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(r, h.diag64.p + h.L.ld, z, n);
         EQC_CHECK_LAUNCH();
         count_launch();
     }
@@ -118,123 +277,222 @@ void precond<float>(Handle& h, const float* r, float* z, int64_t n) {
     if (h.opt.precond == EQC_PC_AMG) {
         mg_apply32(h, r, z);
     } else {
-        k_jacobi<float><<<vgrid(), RED_THREADS, 0, h.stream>>>(r, h.diag32.p + h.L.ld, z, n);
+        k_jacobi<float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(r, h.diag32.p + h.L.ld, z, n);
         EQC_CHECK_LAUNCH();
         count_launch();
     }
 }
 
-// Right-hand-side norm and initial residual; d holds F on row 0 and the guess elsewhere.
-// Returns ||b|| (host) and leaves r64 = b - K_II d_I (rows >= 1, row 0 zero).
-static double setup_residual(Handle& h) {
-    const Layout& L = h.L;
-    const int64_t ld = L.ld;
-    apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);     // r = -(K d)_I
-    apply_K<double>(h.d.p, h.tmp64a.p, args64(h), -1.0, 2, h.stream);  // b on rows 1..4
-    dot64(h, h.tmp64a.p + ld, h.tmp64a.p + ld, 4 * ld, h.scal.p + S_BB);
-    dot64(h, h.r64.p + ld, h.r64.p + ld, L.size() - ld, h.scal.p + S_RR);
-    read_scalars(h);
-    return std::sqrt(h.h_scal[S_BB]);
+// Right-hand side: S->bb = ||b||^2 with b = -K_IF F on rows 1..4 (d holds F on row 0).
+static void setup_rhs(Handle& h) {
+    const int64_t ld = h.L.ld;
+    apply_K<double>(h.d.p, h.tmp64a.p, args64(h), -1.0, 2, h.stream);
+    dot64(h, h.tmp64a.p + ld, h.tmp64a.p + ld, 4 * ld, &h.cg.p->bb);
 }
 
-static int pcg_fp64(Handle& h, double tol, int maxit, double* relres) {
+// Full initial residual: r64 = b - K_II d_I (rows >= 1, row 0 zero), S->rr = ||r||^2, and in
+// mixed precision r32 = (float) r64.
+static void setup_residual_full(Handle& h, bool mixed) {
     const Layout& L = h.L;
     const int64_t ld = L.ld, n = L.size() - ld;
-    const double nb = setup_residual(h);
-    const double reltol = (h.opt.tol_rule == EQC_TOL_R0 ? std::sqrt(h.h_scal[S_RR]) : nb) * tol;
-    double res = std::sqrt(h.h_scal[S_RR]);
+    CGState* S = h.cg.p;
+    apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);     // r = -(K d)_I
+    if (mixed) {
+        k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p,
+                                                             h.red_count.p, &S->rho);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+    } else {
+        dot64(h, h.r64.p + ld, h.r64.p + ld, n, &S->rr);
+    }
+}
+
+// Carried residual: r64 -= K_IF (F - Flast) on rows 1..4 (tmp64b row 0 holds F - Flast).
+static void setup_residual_carry(Handle& h) {
+    const int64_t ld = h.L.ld;
+    apply_K<double>(h.tmp64b.p, h.tmp64c.p, args64(h), -1.0, 2, h.stream);
+    k_carry_rows<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, h.tmp64c.p + ld, 4 * ld,
+                                                        h.red_part.p, h.red_count.p, &h.cg.p->rho);
+    EQC_CHECK_LAUNCH();
+    count_launch();
+}
+
+// One FP64 iteration, ending with the loop decision.
+static void iter_fp64(Handle& h, cudaGraphConditionalHandle hw, int use_cond) {
+    const Layout& L = h.L;
+    const int64_t ld = L.ld, n = L.size() - ld;
+    CGState* S = h.cg.p;
     double* x = h.d.p + ld;
     double* r = h.r64.p + ld;
     double* z = h.z64.p + ld;
     double* u = h.p64.p + ld;
     double* q = h.q64.p + ld;
-    EQC_CUDA(cudaMemsetAsync(h.p64.p, 0, sizeof(double) * L.size(), h.stream));
-    k_set_scalar<<<1, 1, 0, h.stream>>>(h.scal.p, S_RHO, 1.0);
-    count_launch();
-    int it = 0;
-    while (!(it >= maxit || res <= reltol)) {
-        precond<double>(h, r, z, n);
-        k_dot_rho<double><<<vgrid(), RED_THREADS, 0, h.stream>>>(z, r, n, h.red_part.p, h.red_count.p, h.scal.p);
-        k_pupdate<double><<<vgrid(), RED_THREADS, 0, h.stream>>>(z, u, n, h.scal.p);
-        apply_K<double>(h.p64.p, h.q64.p, args64(h), 1.0, 1, h.stream);
-        dot64(h, u, q, n, h.scal.p + S_PQ);
-        k_xr_update<double, double><<<vgrid(), RED_THREADS, 0, h.stream>>>(x, r, u, q, n, h.red_part.p,
-                                                                           h.red_count.p, h.scal.p);
-        EQC_CHECK_LAUNCH();
-        count_launch(3);
-        read_scalars(h);
-        res = std::sqrt(h.h_scal[S_RR]);
-        ++it;
-        if (!std::isfinite(res)) throw Error(EQC_E_NAN, "non-finite residual in CG");
-    }
-    if (relres) *relres = nb > 0 ? res / nb : res;
-    return res <= reltol ? it : -it;
+    precond<double>(h, r, z, n);
+    k_dot_rho<double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, r, n, h.red_part.p, h.red_count.p, &S->rho);
+    k_pupdate<double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho);
+    apply_K<double>(h.p64.p, h.q64.p, args64(h), 1.0, 1, h.stream);
+    dot64(h, u, q, n, &S->pq);
+    k_xr_update<double, double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(x, r, u, q, n, h.red_part.p, h.red_count.p,
+                                                                       &S->rho);
+    k_cg_check<<<1, 1, 0, h.stream>>>(S, hw, use_cond);
+    EQC_CHECK_LAUNCH();
+    count_launch(4);
 }
 
-// CG with reliable updates: FP32 recurrences, FP64 iterate and true residual.
-static int pcg_mixed(Handle& h, double tol, int maxit, double* relres) {
+// Mixed precision: FP32 recurrences of one iteration, ending with the update decision.
+static void iter_mixed_a(Handle& h, double delta, cudaGraphConditionalHandle hi, int use_cond) {
     const Layout& L = h.L;
     const int64_t ld = L.ld, n = L.size() - ld;
-    const double delta = 0.1;
-    const double nb = setup_residual(h);
-    const double reltol = (h.opt.tol_rule == EQC_TOL_R0 ? std::sqrt(h.h_scal[S_RR]) : nb) * tol;
-    double res = std::sqrt(h.h_scal[S_RR]);
-    double* x = h.d.p + ld;
+    CGState* S = h.cg.p;
     float* r = h.r32.p + ld;
     float* z = h.z32.p + ld;
     float* u = h.p32.p + ld;
     float* q = h.q32.p + ld;
     float* y = h.x32.p + ld;   // correction accumulated since the last reliable update
-    EQC_CUDA(cudaMemsetAsync(h.p32.p, 0, sizeof(float) * L.size(), h.stream));
-    EQC_CUDA(cudaMemsetAsync(h.x32.p, 0, sizeof(float) * L.size(), h.stream));
-    k_demote_norm<<<vgrid(), RED_THREADS, 0, h.stream>>>(h.r64.p + ld, r, n, h.red_part.p, h.red_count.p, h.scal.p);
-    k_set_scalar<<<1, 1, 0, h.stream>>>(h.scal.p, S_RHO, 1.0);
-    count_launch(2);
-    double rmax = res;  // largest recurrence residual since the last update
-    int it = 0;
-    while (!(it >= maxit || res <= reltol)) {
-        precond<float>(h, r, z, n);
-        k_dot_rho<float><<<vgrid(), RED_THREADS, 0, h.stream>>>(z, r, n, h.red_part.p, h.red_count.p, h.scal.p);
-        k_pupdate<float><<<vgrid(), RED_THREADS, 0, h.stream>>>(z, u, n, h.scal.p);
-        apply_K<float>(h.p32.p, h.q32.p, args32(h), 1.0f, 1, h.stream);
-        dot32(h, u, q, n, h.scal.p + S_PQ);
-        k_xr_update<float, float><<<vgrid(), RED_THREADS, 0, h.stream>>>(y, r, u, q, n, h.red_part.p,
-                                                                         h.red_count.p, h.scal.p);
-        EQC_CHECK_LAUNCH();
-        count_launch(3);
-        read_scalars(h);
-        double rs = std::sqrt(h.h_scal[S_RR]);
-        ++it;
-        if (!std::isfinite(rs)) throw Error(EQC_E_NAN, "non-finite residual in CG");
-        rmax = std::max(rmax, rs);
-        if (rs < delta * rmax || rs <= reltol || it >= maxit) {
-            // reliable update: x += y ; r = b - K_II x in FP64
-            k_fold<<<vgrid(), RED_THREADS, 0, h.stream>>>(x, y, n);
-            apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);
-            k_demote_norm<<<vgrid(), RED_THREADS, 0, h.stream>>>(h.r64.p + ld, r, n, h.red_part.p, h.red_count.p,
-                                                                 h.scal.p);
-            count_launch(2);
-            read_scalars(h);
-            rs = std::sqrt(h.h_scal[S_RR]);
-            rmax = rs;
-        }
-        res = rs;
-    }
-    if (relres) *relres = nb > 0 ? res / nb : res;
-    return res <= reltol ? it : -it;
+    precond<float>(h, r, z, n);
+    k_dot_rho<float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, r, n, h.red_part.p, h.red_count.p, &S->rho);
+    k_pupdate<float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho);
+    apply_K<float>(h.p32.p, h.q32.p, args32(h), 1.0f, 1, h.stream);
+    dot32(h, u, q, n, &S->pq);
+    k_xr_update<float, float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(y, r, u, q, n, h.red_part.p, h.red_count.p,
+                                                                     &S->rho);
+    k_cg_check_a<<<1, 1, 0, h.stream>>>(S, delta, hi, use_cond);
+    EQC_CHECK_LAUNCH();
+    count_launch(4);
 }
 
-// Solves for d_I given d row 0 = F; returns iterations (negative: maxit reached).
-int qs_solve_device(Handle& h, double tol, int maxit, double* relres) {
+// Reliable update: x += y ; r = b - K_II x in FP64 ; r32 = r ; S->rr = ||r||^2.
+static void update_mixed(Handle& h) {
+    const Layout& L = h.L;
+    const int64_t ld = L.ld, n = L.size() - ld;
+    CGState* S = h.cg.p;
+    k_fold<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.d.p + ld, h.x32.p + ld, n);
+    apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);
+    k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p, h.red_count.p,
+                                                         &S->rho);
+    EQC_CHECK_LAUNCH();
+    count_launch(2);
+}
+
+constexpr double RELIABLE_DELTA = 1e-3;   // default residual-replacement factor
+
+void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry) {
     if (maxit <= 0) maxit = (int)std::min<int64_t>(h.L.size() - h.L.ld, 1 << 30);
-    int it = (h.opt.precision == EQC_MIXED) ? pcg_mixed(h, tol, maxit, relres) : pcg_fp64(h, tol, maxit, relres);
+    const Layout& L = h.L;
+    // the 4-wide vector kernels need whole 8-entry rows (the layout's row pitch)
+    if (L.ld % 8) throw Error(EQC_E_STATE, "row pitch must be a multiple of 8");
+    CGState* S = h.cg.p;
+    const bool mixed = h.opt.precision == EQC_MIXED;
+    carry = carry && mixed;
+    const double delta = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : RELIABLE_DELTA;
+    setup_rhs(h);
+    if (carry) {
+        k_fault_delta<<<(h.F.Nf + 255) / 256, 256, 0, h.stream>>>(h.d.p, h.F.Flast.p, h.tmp64b.p, h.F.Nf);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+        if (graph) {
+            const cudaGraphConditionalHandle hc = cond_handle(h), hf = cond_handle(h);
+            k_setup_select<<<1, 1, 0, h.stream>>>(h.ctrl.p, hc, hf, 1);
+            count_launch();
+            const int64_t t0 = capture_tally();
+            cond_begin(h, cudaGraphCondTypeIf, hc);
+            setup_residual_carry(h);
+            cond_end(h);
+            const int64_t t1 = capture_tally();
+            cond_begin(h, cudaGraphCondTypeIf, hf);
+            setup_residual_full(h, mixed);
+            cond_end(h);
+            if (h.capturing) {
+                h.capturing->k_carry = t1 - t0;
+                h.capturing->k_full = capture_tally() - t1;
+                h.capturing->k_bodies += capture_tally() - t0;
+            }
+        } else {
+            k_setup_select<<<1, 1, 0, h.stream>>>(h.ctrl.p, 0, 0, 0);
+            count_launch();
+            int valid = 0;
+            EQC_CUDA(cudaMemcpyAsync(&valid, &h.ctrl.p->r_valid, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+            EQC_CUDA(cudaStreamSynchronize(h.stream));
+            if (valid) setup_residual_carry(h);
+            else setup_residual_full(h, mixed);
+        }
+    } else {
+        setup_residual_full(h, mixed);
+    }
+    if (mixed) {
+        EQC_CUDA(cudaMemsetAsync(h.p32.p, 0, sizeof(float) * L.size(), h.stream));
+        EQC_CUDA(cudaMemsetAsync(h.x32.p, 0, sizeof(float) * L.size(), h.stream));
+    } else {
+        EQC_CUDA(cudaMemsetAsync(h.p64.p, 0, sizeof(double) * L.size(), h.stream));
+    }
+    if (graph) {
+        // k_cg_init (upstream of the while node) sets the node's first value
+        const cudaGraphConditionalHandle hw = cond_handle(h);
+        k_cg_init<<<1, 1, 0, h.stream>>>(S, tol, maxit, h.opt.tol_rule, hw, 1);
+        count_launch();
+        const int64_t t0 = capture_tally();
+        cond_begin(h, cudaGraphCondTypeWhile, hw);
+        if (mixed) {
+            const cudaGraphConditionalHandle hi = cond_handle(h);
+            iter_mixed_a(h, delta, hi, 1);
+            const int64_t t1 = capture_tally();
+            cond_begin(h, cudaGraphCondTypeIf, hi);
+            update_mixed(h);
+            cond_end(h);
+            const int64_t t2 = capture_tally();
+            k_cg_check_b<<<1, 1, 0, h.stream>>>(S, h.ctrl.p, hw, 1);
+            count_launch();
+            if (h.capturing) {
+                h.capturing->k_update = t2 - t1;
+                h.capturing->k_iter = (t1 - t0) + (capture_tally() - t2);
+                h.capturing->k_bodies += capture_tally() - t0;
+            }
+        } else {
+            iter_fp64(h, hw, 1);
+            if (h.capturing) {
+                h.capturing->k_iter = capture_tally() - t0;
+                h.capturing->k_bodies += capture_tally() - t0;
+            }
+        }
+        cond_end(h);
+    } else {
+        k_cg_init<<<1, 1, 0, h.stream>>>(S, tol, maxit, h.opt.tol_rule, 0, 0);
+        count_launch();
+        const CGState* hs = &read_cg(h);
+        while (hs->done == 0) {
+            if (mixed) {
+                iter_mixed_a(h, delta, 0, 0);
+                hs = &read_cg(h);
+                if (hs->need_update) update_mixed(h);
+                k_cg_check_b<<<1, 1, 0, h.stream>>>(S, h.ctrl.p, 0, 0);
+                count_launch();
+            } else {
+                iter_fp64(h, 0, 0);
+            }
+            hs = &read_cg(h);
+        }
+    }
+    k_cg_finish<<<1, 1, 0, h.stream>>>(S, h.ctrl.p, carry ? 1 : 0);
+    EQC_CHECK_LAUNCH();
+    count_launch();
+}
+
+void invalidate_residual(Handle& h) {
+    EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->r_valid, 0, sizeof(int), h.stream));
+    if (h.h_ctrl) h.h_ctrl->r_valid = 0;
+}
+
+// Solves for d_I given d row 0 = F (eager); returns iterations (negative: maxit reached).
+int qs_solve_device(Handle& h, double tol, int maxit, double* relres) {
+    enqueue_solve(h, tol, maxit, false);
+    const CGState& S = read_cg(h);
     int err = 0;
     EQC_CUDA(cudaMemcpyAsync(&err, &h.ctrl.p->apply_err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
     EQC_CUDA(cudaStreamSynchronize(h.stream));
     if (err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
-    h.cg_iters_total += it < 0 ? -it : it;
-    h.qs_solves_total += 1;
-    return it;
+    if (S.done == 3) throw Error(EQC_E_NAN, "non-finite residual in CG");
+    if (relres) *relres = S.nb > 0 ? S.res / S.nb : S.res;
+    return S.done == 1 ? S.it : -S.it;
 }
 
 }  // namespace eqc

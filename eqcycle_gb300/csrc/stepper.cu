@@ -104,8 +104,9 @@ __global__ void k_zero_list(const int64_t* __restrict__ idx, int n, double* x, d
 // ---------------------------------------------------------------- dynamic kernels
 // vPre on the fault; d += dt v + dt^2/2 a ; v += dt/2 a   (main.jl:299-306)
 __global__ void k_dyn_predict(double* __restrict__ d, double* __restrict__ v, const double* __restrict__ a,
-                              double* __restrict__ vPre_f, int Nf, int64_t n, const Ctrl* C) {
+                              double* __restrict__ vPre_f, int Nf, int64_t n, Ctrl* C) {
     const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
+    if (blockIdx.x == 0 && threadIdx.x == 0) C->r_valid = 0;   // d changes: no carried residual
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double vi = v[i], ai = a[i];
         if (i < Nf) vPre_f[i] = vi;
@@ -435,7 +436,6 @@ void init_state(Handle& h, double V_init) {
     h.tevneb = h.tevne = 0;
     h.idelevne = h.ntvsx = h.nevne = h.slipstart = h.idd = h.it_s = h.it_e = h.rit = 0;
     h.delfref.assign(h.F.Nf, 0.0);
-    h.cg_iters_total = h.qs_solves_total = 0;
     h.initialized = true;
 }
 
@@ -453,86 +453,148 @@ static void fault_columns(Handle& h, std::vector<double>& dF, std::vector<double
     EQC_CUDA(cudaStreamSynchronize(h.stream));
 }
 
-void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
-    if (!h.initialized) throw Error(EQC_E_STATE, "eqc_run before eqc_init");
+// it = it + 1 ; t = t + dt  (main.jl:221-222), dt of this step = C->dt
+__global__ void k_step_begin(Ctrl* C) {
+    C->it += 1;
+    C->t = C->t + C->dt;
+}
+
+// Quasi-static step (main.jl:226-295): two predictor-corrector passes.
+static void enqueue_qs(Handle& h, bool graph) {
     cudaStream_t s = h.stream;
     const Layout& L = h.L;
     const int64_t n = L.size();
-        FaultArgs f = fargs(h, h.bcflag.p);
+    FaultArgs f = fargs(h, h.bcflag.p);
+    EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    k_qs_begin<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.F.Vf0.p, h.F.Vf.p, h.F.Nf, h.ctrl.p);
+    launch_check();
+    count_launch();
+    for (int p1 = 0; p1 < 2; ++p1) {
+        enqueue_solve(h, h.opt.cg_tol, h.opt.cg_maxit, graph, true);
+        apply_K<double>(h.d.p, h.tmp64b.p, args64(h), 1.0, 3, s);  // (K d)[iFlt]
+        k_qs_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.tmp64b.p, h.v.p, h.d.p, h.dPre.p, f, h.ctrl.p, p1 == 0);
+        launch_check();
+        count_launch();
+    }
+    k_qs_end_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.v.p, f, h.ctrl.p);
+    k_qs_end_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.a.p, L.ld, n, h.ctrl.p);
+    count_launch(2);
+    if (h.nCreep) {
+        k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.d.p, h.v.p, nullptr);
+        count_launch();
+    }
+    launch_check();
+}
+
+// Dynamic step (main.jl:297-345): Newmark predictor, K d, boundaries, fault, corrector.
+static void enqueue_dyn(Handle& h) {
+    cudaStream_t s = h.stream;
+    const int64_t n = h.L.size();
+    FaultArgs f = fargs(h, h.bcflag.p);
+    k_dyn_predict<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.F.Nf, n, h.ctrl.p);
+    count_launch();
+    apply_K<double>(h.d.p, h.a.p, args64(h), -1.0, 0, s);
+    k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p, h.BcTC.p,
+                                h.nBcT);
+    k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
+    k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, h.M.p, n, h.ctrl.p);
+    count_launch(3);
+    if (h.nCreep) {
+        k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, h.a.p, nullptr);
+        count_launch();
+    }
+    launch_check();
+}
+
+// One whole time step, ending with the control kernel (Vfmax, regime, next dt).
+static void enqueue_step(Handle& h, int iso, bool graph) {
+    k_step_begin<<<1, 1, 0, h.stream>>>(h.ctrl.p);
+    count_launch();
+    if (iso == 1) enqueue_qs(h, graph);
+    else enqueue_dyn(h);
+    k_control<<<1, FT, 0, h.stream>>>(h.v.p, fargs(h, h.bcflag.p), h.ctrl.p);
+    launch_check();
+    count_launch();
+}
+
+void destroy_graphs(Handle& h) {
+    for (StepGraph& g : h.graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+        g = StepGraph();
+    }
+}
+
+// Captures the step of regime iso (1 quasi-static, 2 dynamic) into a graph, once.
+static StepGraph& step_graph(Handle& h, int iso) {
+    StepGraph& G = h.graphs[iso == 1 ? 0 : 1];
+    if (G.exec) return G;
+    G = StepGraph();
+    h.capturing = &G;
+    capture_counting(true);
+    try {
+        EQC_CUDA(cudaStreamBeginCapture(h.stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(h, iso, true);
+        EQC_CUDA(cudaStreamEndCapture(h.stream, &G.graph));
+    } catch (...) {
+        abort_capture(h);
+        h.capturing = nullptr;
+        throw;
+    }
+    G.k_fixed = capture_tally() - G.k_bodies;
+    capture_counting(false);
+    h.capturing = nullptr;
+    EQC_CUDA(cudaGraphInstantiate(&G.exec, G.graph, 0));
+    return G;
+}
+
+void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
+    if (!h.initialized) throw Error(EQC_E_STATE, "eqc_run before eqc_init");
+    cudaStream_t s = h.stream;
     const int Nf = h.F.Nf;
     const double Vpl = h.Vpl;
     const std::vector<double>& tauo = h.h_tauo;
     const std::vector<double>& FltX = h.h_FltX;
     auto t0 = std::chrono::steady_clock::now();
     eqc_run_stats stats{};
-    const int64_t cg0 = h.cg_iters_total, qs0 = h.qs_solves_total;
     std::vector<double> dF, vF, tauF, seis(3 * std::max(h.nSeis, 1));
     Ctrl& C = *h.h_ctrl;
+    EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+    EQC_CUDA(cudaStreamSynchronize(s));
+    const long long cg0 = C.cg_iters, qs0 = C.cg_solves;
     cudaEvent_t ev0, ev1;
     EQC_CUDA(cudaEventCreate(&ev0));
     EQC_CUDA(cudaEventCreate(&ev1));
     EQC_CUDA(cudaEventRecord(ev0, s));
     while (C.t < t_end && stats.steps < max_steps) {
-        // it = it + 1 ; t = t + dt (main.jl:221-222); dt of this step is C.dt
-        C.it += 1;
-        C.t = C.t + C.dt;
-        const double tnow = C.t;
         if ((int64_t)h.res.time_.size() >= CAP_TIME) throw Error(EQC_E_CAPACITY, "time_ capacity (1900000) exceeded");
-        h.res.time_.push_back(tnow);
-        EQC_CUDA(cudaMemcpyAsync(&h.ctrl.p->t, &C.t, sizeof(double), cudaMemcpyHostToDevice, s));
         const int iso = C.isolver;
-        if (iso == 1) {
-            EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-            k_qs_begin<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.F.Vf0.p, h.F.Vf.p, Nf, h.ctrl.p);
-            launch_check();
-            count_launch();
-            for (int p1 = 0; p1 < 2; ++p1) {
-                double rr = 0;
-                int it = qs_solve_device(h, h.opt.cg_tol, h.opt.cg_maxit, &rr);
-                if (it < 0) throw Error(EQC_E_CG, "CG did not converge within maxit (relres " + std::to_string(rr) + ")");
-                apply_K<double>(h.d.p, h.tmp64b.p, args64(h), 1.0, 3, s);  // (K d)[iFlt]
-                k_qs_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.tmp64b.p, h.v.p, h.d.p, h.dPre.p, f, h.ctrl.p, p1 == 0);
-                launch_check();
-                count_launch();
-            }
-            k_qs_end_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.v.p, f, h.ctrl.p);
-            k_qs_end_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.a.p, L.ld, n, h.ctrl.p);
-            count_launch(2);
-            if (h.nCreep) {
-                k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.d.p, h.v.p, nullptr);
-                count_launch();
-            }
-            launch_check();
-            stats.qs_steps++;
+        const long long it_before = C.cg_iters, up_before = C.cg_updates, ca_before = C.cg_carried,
+                        so_before = C.cg_solves;
+        if (h.opt.use_graphs) {
+            StepGraph& G = step_graph(h, iso);
+            EQC_CUDA(cudaGraphLaunch(G.exec, s));
+            // kernels the replay executes: fixed part plus the conditional bodies that ran
+            EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+            EQC_CUDA(cudaStreamSynchronize(s));
+            const long long carried = C.cg_carried - ca_before;
+            g_launches += G.k_fixed + G.k_iter * (C.cg_iters - it_before) + G.k_update * (C.cg_updates - up_before) +
+                          G.k_carry * carried + G.k_full * (C.cg_solves - so_before - carried);
         } else {
-            k_dyn_predict<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, Nf, n, h.ctrl.p);
-            count_launch();
-            apply_K<double>(h.d.p, h.a.p, args64(h), -1.0, 0, s);
-            k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p,
-                                        h.BcTC.p, h.nBcT);
-            k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
-            k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, h.M.p, n, h.ctrl.p);
-            count_launch(3);
-            if (h.nCreep) {
-                k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, h.a.p, nullptr);
-                count_launch();
-            }
-            launch_check();
-            stats.dyn_steps++;
+            enqueue_step(h, iso, false);
+            EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+            EQC_CUDA(cudaStreamSynchronize(s));
         }
-        k_control<<<1, FT, 0, s>>>(h.v.p, f, h.ctrl.p);
-        launch_check();
-        count_launch();
-        // host mirror of the control block
-        const double t_keep = C.t;
-        const long long it_keep = C.it;
-        EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
-        EQC_CUDA(cudaStreamSynchronize(s));
-        C.t = t_keep;
-        C.it = it_keep;
+        if (iso == 1) stats.qs_steps++;
+        else stats.dyn_steps++;
+        const double tnow = C.t;
+        h.res.time_.push_back(tnow);
         if (C.fail != 0x7fffffff)
             throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(C.fail));
         if (C.apply_err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
+        if (C.cg_fail & 2) throw Error(EQC_E_NAN, "non-finite residual in CG");
+        if (C.cg_fail & 1)
+            throw Error(EQC_E_CG, "CG did not converge within maxit (relres " + std::to_string(C.cg_last_relres) + ")");
         const double Vfmax = C.Vfmax;
         if (!std::isfinite(Vfmax)) throw Error(EQC_E_NAN, "non-finite slip rate");
         // ---- outputs (main.jl:361-436) ----
@@ -621,8 +683,8 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     stats.gpu_ms = gms;
-    stats.cg_iters = h.cg_iters_total - cg0;
-    stats.qs_solves = h.qs_solves_total - qs0;
+    stats.cg_iters = C.cg_iters - cg0;
+    stats.qs_solves = C.cg_solves - qs0;
     stats.t = C.t;
     stats.dt = C.dt;
     stats.isolver = C.isolver;

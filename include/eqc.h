@@ -83,6 +83,11 @@ typedef struct {
     int32_t device;      /* CUDA device ordinal                          */
     int32_t use_graphs;  /* capture the per-step work in CUDA graphs     */
     int32_t verbose;     /* print "Time (yr) = ..." every 500 steps (main.jl:425-427) */
+    /* solver tuning (0 = default) */
+    double reliable_delta;  /* mixed precision: FP64 residual replacement whenever the
+                               recurrence residual fell by this factor (default 1e-3)  */
+    int32_t mg_degree;      /* Chebyshev smoothing steps per level, pre and post (default 4) */
+    int32_t mg_coarse_max;  /* largest coarsest level, solved densely (default 2048 unknowns) */
 } eqc_options;
 
 typedef struct eqc_handle eqc_handle;
@@ -170,7 +175,9 @@ eqc_status eqc_run(eqc_handle* h, int64_t max_steps, double t_end, eqc_run_stats
  * [nglob], "psi", "tau" [FltNglob].  eqc_set_state writes it back. */
 eqc_status eqc_get_state(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
-/* Scalars "t", "dt", "isolver", "it" (and, read-only, "cg_iters", "qs_solves").
+/* Scalars "t", "dt", "isolver", "it" (and, read-only, the solver counters "cg_iters",
+ * "qs_solves", "cg_updates" (reliable updates), "cg_carried" (solves that started from
+ * the residual the previous solve left)).
  * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);

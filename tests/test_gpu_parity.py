@@ -162,3 +162,43 @@ def test_multigrid_time_loop_matches_oracle(eqclib, oracle_mod):
     assert st["steps"] == 30
     for k in ("d", "v", "psi", "tau"):
         assert rel(got[k], ref[k]) <= 1e-8, k
+
+
+@pytest.mark.parametrize("precision", [EQC_FP64, EQC_MIXED], ids=["fp64", "mixed"])
+def test_graph_step_equals_eager_step(eqclib, precision):
+    """A step replayed from its CUDA graph (device-driven CG loop in conditional nodes) runs
+    the same kernels in the same order as the host-driven step: bitwise equal state and the
+    same iteration counts, through quasi-static and dynamic steps."""
+    cfg = preset("dz40").replace(V_init=2e-2)
+    P = set_parameters(cfg)
+    out = []
+    for graphs in (0, 1):
+        with Solver(P, precision=precision, precond=EQC_PC_AMG, use_graphs=graphs) as s:
+            s.init(cfg.V_init)
+            st = s.run(12)
+            out.append((st, {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}))
+    (st0, x0), (st1, x1) = out
+    assert st0["qs_steps"] >= 1 and st0["dyn_steps"] >= 1, st0
+    for k in ("steps", "qs_steps", "dyn_steps", "cg_iters", "qs_solves", "isolver"):
+        assert st0[k] == st1[k], k
+    for k in x0:
+        assert np.array_equal(x0[k], x1[k]), k
+
+
+def test_mixed_time_loop_matches_fp64_oracle(eqclib, oracle_mod):
+    """Mixed precision in the time loop (FP32 apply and multigrid inside the FP64
+    reliable-update CG, residual carried from one solve to the next): the state after 15
+    quasi-static steps agrees with the FP64 oracle solved tightly."""
+    cfg = reference_config(res=1)
+    P = set_parameters(cfg)
+    o = oracle_mod.Oracle(cfg)
+    o.run(15, qs_mode=1, qs_tol=1e-13)
+    with Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG, cg_tol=1e-10) as s:
+        s.init(cfg.V_init)
+        st = s.run(15)
+        got = {k: s.state(k) for k in ("d", "v", "psi", "tau")}
+        carried = s.scalar("cg_carried")
+    assert st["qs_steps"] == 15
+    assert carried >= st["qs_solves"] - 2     # every solve but the first carries
+    for k in ("d", "v", "psi", "tau"):
+        assert rel(got[k], o.state(k)) <= 1e-6, k
