@@ -301,8 +301,9 @@ def bench_kernel(args):
     P = set_parameters(preset(args.workload))
     nglob, Nel = P.int_.nglob, P.int_.Nel
     peak, kind = measured_peaks()
-    with Solver(P, precond=EQC_PC_JACOBI) as s:
-        out = {"workload": args.workload, "nodes": nglob, "elements": Nel, "peak_gbs": peak, "peak_kind": kind}
+    with Solver(P, precond=EQC_PC_JACOBI, apply_variant=args.apply_variant) as s:
+        out = {"workload": args.workload, "nodes": nglob, "elements": Nel, "peak_gbs": peak, "peak_kind": kind,
+               "apply_variant": args.apply_variant}
         for name, dt, es in (("f32", 1, 4), ("f64", 0, 8)):
             if args.dtype not in ("both", name):
                 continue
@@ -325,6 +326,8 @@ def main():
     ap.add_argument("--kernel-only", action="store_true", help="time the stiffness apply alone")
     ap.add_argument("--dtype", default="both", choices=["both", "f32", "f64"])
     ap.add_argument("--nrep", type=int, default=20)
+    ap.add_argument("--apply-variant", type=int, default=0,
+                    help="stiffness apply kernel: 0 persistent TMA pipeline, 1 one tile per CTA, 2 plain loads")
     args = ap.parse_args()
     if args.kernel_only:
         bench_kernel(args)

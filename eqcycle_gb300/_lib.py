@@ -46,7 +46,8 @@ class EqcOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("precond", C.c_int32), ("guess", C.c_int32), ("tol_rule", C.c_int32),
                 ("cg_tol", C.c_double), ("cg_maxit", C.c_int32), ("device", C.c_int32),
                 ("use_graphs", C.c_int32), ("verbose", C.c_int32),
-                ("reliable_delta", C.c_double), ("mg_degree", C.c_int32), ("mg_coarse_max", C.c_int32)]
+                ("reliable_delta", C.c_double), ("mg_degree", C.c_int32), ("mg_coarse_max", C.c_int32),
+                ("mg_cluster_max", C.c_int32), ("apply_variant", C.c_int32)]
 
 
 class EqcRunStats(C.Structure):

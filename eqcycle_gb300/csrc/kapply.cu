@@ -15,6 +15,7 @@
 // shared memory.
 #include "model.h"
 #include <cstdlib>
+#include <algorithm>
 
 namespace eqc {
 
@@ -377,6 +378,82 @@ __global__ void __launch_bounds__(NT) k_apply_tma(const __grid_constant__ CUtens
     lines_compute<T, TEX, TEY, NT, UPT, WP>(us, ws, ys, cx, cy, y, A, ex0, ey0, sign, zero_row0);
 }
 
+// ---- persistent, pipelined version ---------------------------------------------------------
+// A grid of a few CTAs per SM walks the tile list (tile t = blockIdx.x + k*gridDim.x); each CTA
+// keeps PSTAGES tiles in flight: the node and element tiles of tile i+PSTAGES are fetched by
+// TMA while tile i is computed, so HBM streams continuously instead of once per CTA lifetime.
+constexpr int PSTAGES = 3;
+
+template <class T, int TEX, int TEY>
+struct PipeLayout {
+    static constexpr int UY = 4 * TEY + 5, OX = 4 * TEX, OY = 4 * TEY, EX = TEX + 1, EY = TEY + 1;
+    static constexpr int WP = WPad<T>::v;
+    static constexpr int U_BYTES = UY * UPT * (int)sizeof(T);            // node tile
+    static constexpr int W_BYTES = EY * EX * WP * (int)sizeof(T);        // element tile
+    static constexpr int STAGE = ((U_BYTES + 127) / 128 + (W_BYTES + 127) / 128) * 128;
+    static constexpr int WORK = (OY * OX + OY * EX + EY * OX) * (int)sizeof(T);
+    static constexpr int BYTES = PSTAGES * STAGE + ((WORK + 127) / 128) * 128 + 8 * PSTAGES;
+};
+
+template <class T, int TEX, int TEY, int NT>
+__global__ void __launch_bounds__(NT) k_apply_pipe(const __grid_constant__ CUtensorMap umap,
+                                                   const __grid_constant__ CUtensorMap wmap, T* __restrict__ y,
+                                                   ApplyArgs<T> A, T sign, int zero_row0, int ntx, int ntiles) {
+    using PL = PipeLayout<T, TEX, TEY>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    T* ys = reinterpret_cast<T*>(smem + PSTAGES * PL::STAGE);
+    T* cxs = ys + PL::OY * PL::OX;
+    T* cys = cxs + PL::OY * PL::EX;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + PSTAGES * PL::STAGE + ((PL::WORK + 127) / 128) * 128);
+    auto us_of = [&](int st) { return reinterpret_cast<T*>(smem + st * PL::STAGE); };
+    auto ws_of = [&](int st) { return reinterpret_cast<T*>(smem + st * PL::STAGE + ((PL::U_BYTES + 127) / 128) * 128); };
+    auto issue = [&](int t, int st) {
+        const int ex0 = (t % ntx) * TEX, ey0 = (t / ntx) * TEY;
+        mbar_expect_tx(&bar[st], (uint32_t)(PL::U_BYTES + PL::W_BYTES));
+        tma_load_2d(us_of(st), &umap, &bar[st], 4 * ex0 - 4, 4 * ey0 - 4);
+        tma_load_2d(ws_of(st), &wmap, &bar[st], (ex0 - 1) * PL::WP, ey0 - 1);
+    };
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < PSTAGES; ++st) mbar_init(&bar[st], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int st = 0; st < PSTAGES; ++st) {
+            const int t = blockIdx.x + st * gridDim.x;
+            if (t < ntiles) issue(t, st);
+        }
+    int i = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+        const int st = i % PSTAGES;
+        const uint32_t parity = (uint32_t)((i / PSTAGES) & 1);
+        bool done = false;
+        for (int it = 0; it < MBAR_SPIN_LIMIT && !done; ++it) done = mbar_try_wait(&bar[st], parity);
+        if (__syncthreads_or(!done)) {
+            // give up: flag it, wait (bounded) for every copy still targeting this CTA, leave
+            if (threadIdx.x == 0) {
+                if (A.err) atomicExch(A.err, 1);
+                int j = i;
+                for (int tt = t; tt < ntiles && j < i + PSTAGES; tt += gridDim.x, ++j) {
+                    const int sj = j % PSTAGES;
+                    const uint32_t pj = (uint32_t)((j / PSTAGES) & 1);
+                    for (int it = 0; it < MBAR_SPIN_LIMIT; ++it)
+                        if (mbar_try_wait(&bar[sj], pj)) break;
+                }
+            }
+            return;
+        }
+        const int ex0 = (t % ntx) * TEX, ey0 = (t / ntx) * TEY;
+        lines_compute<T, TEX, TEY, NT, UPT, PL::WP>(us_of(st), ws_of(st), ys, cxs, cys, y, A, ex0, ey0, sign,
+                                                    zero_row0);
+        __syncthreads();   // every thread is done with this stage and with ys/cx/cy
+        if (threadIdx.x == 0) {
+            const int tn = t + PSTAGES * gridDim.x;
+            if (tn < ntiles) issue(tn, st);
+        }
+    }
+}
+
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                      const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                      CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -455,6 +532,22 @@ void tma_init(Handle& h) {
     c.ok = ok;
 }
 
+// CTAs of the pipelined apply: as many as fit on every SM at once.
+static int g_pipe_blocks[2] = {0, 0};
+template <class T>
+static int pipe_blocks() { return g_pipe_blocks[sizeof(T) == 8 ? 1 : 0]; }
+
+template <class T>
+static void pipe_setup() {
+    const int bytes = PipeLayout<T, LTEX, LTEY>::BYTES;
+    EQC_CUDA(cudaFuncSetAttribute(k_apply_pipe<T, LTEX, LTEY, LNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    int per_sm = 0, dev = 0, nsm = 0;
+    EQC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_pipe<T, LTEX, LTEY, LNT>, LNT, bytes));
+    EQC_CUDA(cudaGetDevice(&dev));
+    EQC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    g_pipe_blocks[sizeof(T) == 8 ? 1 : 0] = std::max(1, per_sm) * nsm;
+}
+
 void set_H(const double* H, cudaStream_t s) {
     float hf[25];
     for (int k = 0; k < 25; ++k) hf[k] = (float)H[k];
@@ -466,15 +559,22 @@ void set_H(const double* H, cudaStream_t s) {
                                   (int)apply_smem<double>()));
     EQC_CUDA(cudaFuncSetAttribute(k_apply<float, TEX, TEY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)apply_smem<float>()));
+    pipe_setup<float>();
+    pipe_setup<double>();
 }
 
 template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s) {
     if (mode <= 1) {
         dim3 grid(A.L.NelX / LTEX + 1, A.L.NelY / LTEY + 1);
-        const CUtensorMap* um = A.tma ? tma_umap<T>(*A.tma, x, A.L) : nullptr;
-        if (um) {
+        const CUtensorMap* um = (A.tma && A.variant != 2) ? tma_umap<T>(*A.tma, x, A.L) : nullptr;
+        if (um && A.variant == 1) {
             k_apply_tma<T, LTEX, LTEY, LNT><<<grid, LNT, 0, s>>>(*um, tma_wmap<T>(*A.tma), y, A, sign, mode == 1 ? 1 : 0);
+        } else if (um) {
+            const int ntx = (int)grid.x, ntiles = (int)(grid.x * grid.y);
+            const int nblk = std::min(ntiles, pipe_blocks<T>());
+            k_apply_pipe<T, LTEX, LTEY, LNT><<<nblk, LNT, PipeLayout<T, LTEX, LTEY>::BYTES, s>>>(
+                *um, tma_wmap<T>(*A.tma), y, A, sign, mode == 1 ? 1 : 0, ntx, ntiles);
         } else {
             k_apply_lines<T, LTEX, LTEY, LNT><<<grid, LNT, 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
         }

@@ -134,10 +134,10 @@ template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s);
 
 inline ApplyArgs<double> args64(Handle& h) {
-    return {h.W64.p, h.c1, h.c2, h.L, h.W64p.p, &h.ctrl.p->apply_err, &h.tma};
+    return {h.W64.p, h.c1, h.c2, h.L, h.W64p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant};
 }
 inline ApplyArgs<float> args32(Handle& h) {
-    return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma};
+    return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant};
 }
 void tma_init(Handle& h);
 

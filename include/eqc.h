@@ -88,6 +88,10 @@ typedef struct {
                                recurrence residual fell by this factor (default 1e-3)  */
     int32_t mg_degree;      /* Chebyshev smoothing steps per level, pre and post (default 4) */
     int32_t mg_coarse_max;  /* largest coarsest level, solved densely (default 2048 unknowns) */
+    int32_t mg_cluster_max; /* > 0: levels with at most this many grid points run as one
+                               thread-block-cluster launch (default 0: off)            */
+    int32_t apply_variant;  /* stiffness apply kernel: 0 persistent TMA pipeline (default),
+                               1 one tile per CTA by TMA, 2 plain loads                */
 } eqc_options;
 
 typedef struct eqc_handle eqc_handle;
