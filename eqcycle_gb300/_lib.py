@@ -19,7 +19,7 @@ STATUS = {0: "EQC_OK", 1: "EQC_E_ARG", 2: "EQC_E_CUDA", 3: "EQC_E_NR", 4: "EQC_E
           6: "EQC_E_CAPACITY", 7: "EQC_E_TIMEOUT", 8: "EQC_E_NOMEM", 9: "EQC_E_STATE", 10: "EQC_E_NOGPU"}
 EQC_FP64, EQC_MIXED = 0, 1
 EQC_PC_AMG, EQC_PC_JACOBI = 0, 1
-EQC_GUESS_PREVIOUS, EQC_GUESS_LEARNED = 0, 1
+EQC_GUESS_PREVIOUS, EQC_GUESS_LEARNED, EQC_GUESS_EXTRAPOLATE = 0, 1, 2
 EQC_TOL_RHS, EQC_TOL_R0 = 0, 1
 
 _dp = C.POINTER(C.c_double)

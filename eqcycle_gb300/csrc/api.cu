@@ -125,7 +125,7 @@ static void create(Handle& h, const eqc_model& m) {
     for (DBuf<double>* b : {&h.M, &h.d, &h.v, &h.a, &h.dPre, &h.tmp64a, &h.tmp64b, &h.tmp64c, &h.r64, &h.z64, &h.p64,
                              &h.q64})
         b->alloc(N);
-    for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32}) b->alloc(N);
+    for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32, &h.g32}) b->alloc(N);
     h.M.upload(Mlay.data(), N, s);
     std::vector<double> dg = diag_K(h, m.W);
     for (int64_t i = 0; i < N; ++i)   // fault row and row padding are not part of the system

@@ -35,6 +35,8 @@ struct Ctrl {
     double cg_last_relres; // ||r|| / ||b|| of the last solve
     int r_valid;           // r64 holds the FP64 true residual of d with fault row Flast
                            // (mixed precision: carried into the next solve)
+    double dt_prev;        // dt of the step before the current one
+    int qs_prev;           // the last step was quasi-static: dPre holds the solution before it
 };
 
 // Device-resident scalars of one CG solve.
@@ -110,6 +112,7 @@ struct Handle {
     // CG work vectors
     DBuf<double> r64, z64, p64, q64;
     DBuf<float> r32, z32, p32, q32, x32;
+    DBuf<float> g32;      // initial-guess increment added to d before the first solve of a step
     // multigrid
     MGHier* mg = nullptr;     // owned; released by mg_destroy
     bool initialized = false;
@@ -150,7 +153,9 @@ void dot32(Handle& h, const float* x, const float* y, int64_t n, double* out_dev
 // becomes a conditional while node; otherwise the host drives it (one sync per iteration).
 // carry: mixed precision in the time loop may start from the residual the previous solve
 // left (r_valid), updated for the change of the fault row, instead of a full FP64 apply.
-void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry = false);
+// guess: the FP32 increment g already added to d (rows >= 1); a carried residual is then
+// corrected by -K_II g (FP32 apply: the first reliable update recomputes r in FP64).
+void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry = false, const float* guess = nullptr);
 // Marks the carried residual stale (after the state was changed from outside the loop).
 void invalidate_residual(Handle& h);
 int qs_solve_device(Handle& h, double tol, int maxit, double* relres);

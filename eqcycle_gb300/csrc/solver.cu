@@ -243,6 +243,27 @@ __global__ void __launch_bounds__(VEC_THREADS) k_carry_rows(double* __restrict__
     finish_reduction(s, part, count, sh, [&](double tt) { S[S_RR] += tt; });
 }
 
+// Carried residual after the guess increment g: r32 -= K_II g (t = K_II g in FP32),
+// S_RR = ||r32||^2.
+__global__ void __launch_bounds__(VEC_THREADS) k_guess_residual(float* __restrict__ r32, const float* __restrict__ t,
+                                                                int64_t n, double* part, unsigned* count, double* S) {
+    __shared__ double sh[32];
+    DotAcc<float> acc;
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        float rr[4], tt[4];
+        ld4(r32 + i, rr);
+        ld4(t + i, tt);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            rr[k] -= tt[k];
+            acc.add(rr[k], rr[k]);
+        }
+        st4(r32 + i, rr);
+    }
+    const double s = block_sum(acc.value(), sh);
+    finish_reduction(s, part, count, sh, [&](double tt2) { S[S_RR] = tt2; });
+}
+
 // Chooses the residual set-up of a solve: carry (r_valid) or a full FP64 apply.
 __global__ void k_setup_select(Ctrl* C, cudaGraphConditionalHandle hc, cudaGraphConditionalHandle hf, int use_cond) {
     const unsigned v = C->r_valid ? 1u : 0u;
@@ -307,14 +328,22 @@ static void setup_residual_full(Handle& h, bool mixed) {
     }
 }
 
-// Carried residual: r64 -= K_IF (F - Flast) on rows 1..4 (tmp64b row 0 holds F - Flast).
-static void setup_residual_carry(Handle& h) {
-    const int64_t ld = h.L.ld;
+// Carried residual: r64 -= K_IF (F - Flast) on rows 1..4 (tmp64b row 0 holds F - Flast), and
+// with a guess increment g in d: r32 -= K_II g (the first reliable update recomputes r64).
+static void setup_residual_carry(Handle& h, const float* guess) {
+    const int64_t ld = h.L.ld, n = h.L.size() - ld;
     apply_K<double>(h.tmp64b.p, h.tmp64c.p, args64(h), -1.0, 2, h.stream);
     k_carry_rows<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, h.tmp64c.p + ld, 4 * ld,
                                                         h.red_part.p, h.red_count.p, &h.cg.p->rho);
     EQC_CHECK_LAUNCH();
     count_launch();
+    if (guess) {
+        apply_K<float>(guess, h.q32.p, args32(h), 1.0f, 1, h.stream);
+        k_guess_residual<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r32.p + ld, h.q32.p + ld, n, h.red_part.p,
+                                                                h.red_count.p, &h.cg.p->rho);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+    }
 }
 
 // One FP64 iteration, ending with the loop decision.
@@ -376,7 +405,7 @@ static void update_mixed(Handle& h) {
 
 constexpr double RELIABLE_DELTA = 1e-3;   // default residual-replacement factor
 
-void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry) {
+void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry, const float* guess) {
     if (maxit <= 0) maxit = (int)std::min<int64_t>(h.L.size() - h.L.ld, 1 << 30);
     const Layout& L = h.L;
     // the 4-wide vector kernels need whole 8-entry rows (the layout's row pitch)
@@ -396,7 +425,7 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry) {
             count_launch();
             const int64_t t0 = capture_tally();
             cond_begin(h, cudaGraphCondTypeIf, hc);
-            setup_residual_carry(h);
+            setup_residual_carry(h, guess);
             cond_end(h);
             const int64_t t1 = capture_tally();
             cond_begin(h, cudaGraphCondTypeIf, hf);
@@ -413,7 +442,7 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry) {
             int valid = 0;
             EQC_CUDA(cudaMemcpyAsync(&valid, &h.ctrl.p->r_valid, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
             EQC_CUDA(cudaStreamSynchronize(h.stream));
-            if (valid) setup_residual_carry(h);
+            if (valid) setup_residual_carry(h, guess);
             else setup_residual_full(h, mixed);
         }
     } else {
@@ -479,7 +508,8 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry) {
 
 void invalidate_residual(Handle& h) {
     EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->r_valid, 0, sizeof(int), h.stream));
-    if (h.h_ctrl) h.h_ctrl->r_valid = 0;
+    EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->qs_prev, 0, sizeof(int), h.stream));
+    if (h.h_ctrl) h.h_ctrl->r_valid = h.h_ctrl->qs_prev = 0;
 }
 
 // Solves for d_I given d row 0 = F (eager); returns iterations (negative: maxit reached).

@@ -34,6 +34,26 @@ __global__ void __launch_bounds__(FNT) k_qs_begin(double* __restrict__ d, const 
     }
 }
 
+// Start of a quasi-static step on the bulk rows: dPre = d (main.jl:230) and, when asked and the
+// last step was quasi-static, the extrapolated initial guess d += g with
+// g = (dt / dt_prev) (d - dPre_old) (g also kept in FP32 for the residual correction).
+__global__ void k_qs_begin_bulk(double* __restrict__ d, double* __restrict__ dPre, float* __restrict__ g, int64_t n,
+                                int64_t ld, int extrap, const Ctrl* C) {
+    const bool use = extrap && C->qs_prev && C->dt_prev > 0;
+    const double ratio = use ? C->dt / C->dt_prev : 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double dn = d[i], dp = dPre[i];
+        dPre[i] = dn;
+        if (i >= ld) {
+            const double gi = use ? ratio * (dn - dp) : 0.0;
+            d[i] = dn + gi;
+            g[i] = (float)gi;
+        } else {
+            g[i] = 0.f;
+        }
+    }
+}
+
 // After a pass's solve (main.jl:265-279): tau1 = -(K d)[iFlt]/FltB with a[FltIglobBC] = 0,
 // slrFunc!, Vf1[iFBC] = Vpl, Vf = (Vf0+Vf1)/2, v[iFlt] = (Vf - Vpl)/2.  If next_F, also
 // writes the next pass's F into d[iFlt].
@@ -106,7 +126,10 @@ __global__ void k_zero_list(const int64_t* __restrict__ idx, int n, double* x, d
 __global__ void k_dyn_predict(double* __restrict__ d, double* __restrict__ v, const double* __restrict__ a,
                               double* __restrict__ vPre_f, int Nf, int64_t n, Ctrl* C) {
     const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
-    if (blockIdx.x == 0 && threadIdx.x == 0) C->r_valid = 0;   // d changes: no carried residual
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // d changes: no carried residual, no QS history
+        C->r_valid = 0;
+        C->qs_prev = 0;
+    }
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double vi = v[i], ai = a[i];
         if (i < Nf) vPre_f[i] = vi;
@@ -221,6 +244,8 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
         } else {
             dt = C->dtmin;
         }
+        C->dt_prev = C->dt;
+        if (iso == 1) C->qs_prev = 1;
         C->dt = dt;
     }
 }
@@ -465,12 +490,18 @@ static void enqueue_qs(Handle& h, bool graph) {
     const Layout& L = h.L;
     const int64_t n = L.size();
     FaultArgs f = fargs(h, h.bcflag.p);
-    EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    const bool extrap = h.opt.guess == EQC_GUESS_EXTRAPOLATE;
+    if (extrap) {
+        k_qs_begin_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.g32.p, n, L.ld, 1, h.ctrl.p);
+        count_launch();
+    } else {
+        EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    }
     k_qs_begin<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.F.Vf0.p, h.F.Vf.p, h.F.Nf, h.ctrl.p);
     launch_check();
     count_launch();
     for (int p1 = 0; p1 < 2; ++p1) {
-        enqueue_solve(h, h.opt.cg_tol, h.opt.cg_maxit, graph, true);
+        enqueue_solve(h, h.opt.cg_tol, h.opt.cg_maxit, graph, true, (p1 == 0 && extrap) ? h.g32.p : nullptr);
         apply_K<double>(h.d.p, h.tmp64b.p, args64(h), 1.0, 3, s);  // (K d)[iFlt]
         k_qs_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.tmp64b.p, h.v.p, h.d.p, h.dPre.p, f, h.ctrl.p, p1 == 0);
         launch_check();

@@ -69,14 +69,16 @@ enum { EQC_FP64 = 0,      /* plain FP64: every kernel in double precision       
                              reliable-update CG; FP64 friction, state, Newmark   */
 enum { EQC_PC_AMG = 0, EQC_PC_JACOBI = 1 };
 enum { EQC_GUESS_PREVIOUS = 0,   /* dnew .= d[FltNI] (src/main.jl:241)            */
-       EQC_GUESS_LEARNED = 1 };  /* learned initial guess, previous-step fallback  */
+       EQC_GUESS_LEARNED = 1,    /* learned initial guess, previous-step fallback  */
+       EQC_GUESS_EXTRAPOLATE = 2 }; /* d_n + (dt_n / dt_{n-1}) (d_n - d_{n-1}) after a
+                                      quasi-static step, previous-step otherwise  */
 enum { EQC_TOL_RHS = 0,          /* stop when ||r|| <= tol*||b|| (IterativeSolvers 0.8 rule) */
        EQC_TOL_R0 = 1 };         /* stop when ||r|| <= tol*||r0||                  */
 
 typedef struct {
     int32_t precision;   /* EQC_FP64 / EQC_MIXED                         */
     int32_t precond;     /* EQC_PC_AMG / EQC_PC_JACOBI                   */
-    int32_t guess;       /* EQC_GUESS_PREVIOUS / EQC_GUESS_LEARNED       */
+    int32_t guess;       /* EQC_GUESS_PREVIOUS / _LEARNED / _EXTRAPOLATE  */
     int32_t tol_rule;    /* EQC_TOL_RHS / EQC_TOL_R0                     */
     double cg_tol;       /* main.jl:256 uses 1e-6; the workloads use 1e-8 */
     int32_t cg_maxit;    /* <= 0: size of the system (IterativeSolvers default) */

@@ -164,8 +164,9 @@ def test_multigrid_time_loop_matches_oracle(eqclib, oracle_mod):
         assert rel(got[k], ref[k]) <= 1e-8, k
 
 
-@pytest.mark.parametrize("precision", [EQC_FP64, EQC_MIXED], ids=["fp64", "mixed"])
-def test_graph_step_equals_eager_step(eqclib, precision):
+@pytest.mark.parametrize("precision,guess", [(EQC_FP64, 0), (EQC_MIXED, 0), (EQC_MIXED, 2)],
+                         ids=["fp64", "mixed", "mixed-extrapolate"])
+def test_graph_step_equals_eager_step(eqclib, precision, guess):
     """A step replayed from its CUDA graph (device-driven CG loop in conditional nodes) runs
     the same kernels in the same order as the host-driven step: bitwise equal state and the
     same iteration counts, through quasi-static and dynamic steps."""
@@ -173,7 +174,7 @@ def test_graph_step_equals_eager_step(eqclib, precision):
     P = set_parameters(cfg)
     out = []
     for graphs in (0, 1):
-        with Solver(P, precision=precision, precond=EQC_PC_AMG, use_graphs=graphs) as s:
+        with Solver(P, precision=precision, precond=EQC_PC_AMG, use_graphs=graphs, guess=guess) as s:
             s.init(cfg.V_init)
             st = s.run(12)
             out.append((st, {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}))
@@ -185,7 +186,8 @@ def test_graph_step_equals_eager_step(eqclib, precision):
         assert np.array_equal(x0[k], x1[k]), k
 
 
-def test_mixed_time_loop_matches_fp64_oracle(eqclib, oracle_mod):
+@pytest.mark.parametrize("guess", [0, 2], ids=["previous", "extrapolate"])
+def test_mixed_time_loop_matches_fp64_oracle(eqclib, oracle_mod, guess):
     """Mixed precision in the time loop (FP32 apply and multigrid inside the FP64
     reliable-update CG, residual carried from one solve to the next): the state after 15
     quasi-static steps agrees with the FP64 oracle solved tightly."""
@@ -193,7 +195,7 @@ def test_mixed_time_loop_matches_fp64_oracle(eqclib, oracle_mod):
     P = set_parameters(cfg)
     o = oracle_mod.Oracle(cfg)
     o.run(15, qs_mode=1, qs_tol=1e-13)
-    with Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG, cg_tol=1e-10) as s:
+    with Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG, cg_tol=1e-10, guess=guess) as s:
         s.init(cfg.V_init)
         st = s.run(15)
         got = {k: s.state(k) for k in ("d", "v", "psi", "tau")}
