@@ -65,7 +65,9 @@ _lib: Optional[C.CDLL] = None
 EXPORTS = ["eqc_default_options", "eqc_create", "eqc_destroy", "eqc_last_error", "eqc_apply_K", "eqc_qs_solve",
            "eqc_slrFunc", "eqc_FBC", "eqc_dtevol", "eqc_dtevol_noalloc", "eqc_init", "eqc_run", "eqc_get_state", "eqc_set_state",
            "eqc_get_scalar", "eqc_set_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
-           "eqc_time_apply", "eqc_launch_count", "eqc_sync"]
+           "eqc_time_apply", "eqc_launch_count", "eqc_sync", "eqc_guess_shape", "eqc_guess_init",
+           "eqc_guess_get_params", "eqc_guess_set_params", "eqc_guess_log", "eqc_guess_pairs", "eqc_guess_train",
+           "eqc_guess_eval", "eqc_guess_grad"]
 
 
 def lib() -> C.CDLL:
@@ -104,10 +106,28 @@ def lib() -> C.CDLL:
     L.eqc_launch_count.restype = I64
     L.eqc_launch_count.argtypes = [P]
     L.eqc_sync.argtypes = [P]
+    _fp = C.POINTER(C.c_float)
+    U64 = C.c_uint64
+    L.eqc_guess_shape.argtypes = [P, C.POINTER(I32), C.POINTER(I32), C.POINTER(I64)]
+    L.eqc_guess_init.argtypes = [P, U64]
+    L.eqc_guess_get_params.argtypes = [P, _fp]
+    L.eqc_guess_set_params.argtypes = [P, _fp]
+    L.eqc_guess_log.argtypes = [P, I64]
+    L.eqc_guess_pairs.argtypes = [P, _fp, _fp, C.POINTER(I64)]
+    L.eqc_guess_train.argtypes = [P, _fp, _fp, I64, I32, D, I32, U64, _dp]
+    L.eqc_guess_eval.argtypes = [P, _fp, _fp, I64, _dp, _fp]
+    L.eqc_guess_grad.argtypes = [P, _fp, _fp, I64, _fp, _dp]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L
     return L
+
+
+def fptr(a):
+    """float* of a float32 array (None -> NULL)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 def dptr(a: np.ndarray):

@@ -1,6 +1,7 @@
 // C ABI of libeqc (include/eqc.h): model upload, reference-numbering <-> layout
 // permutation, host-array entry points.
 #include "model.h"
+#include "learn.h"
 #include <cmath>
 #include <cstring>
 #include <algorithm>
@@ -10,6 +11,7 @@ namespace eqc {
 Handle::~Handle() {
     destroy_graphs(*this);
     mg_destroy(*this);
+    delete net;
     if (h_ctrl) cudaFreeHost(h_ctrl);
     if (h_scal) cudaFreeHost(h_scal);
     if (h_cg) cudaFreeHost(h_cg);

@@ -60,8 +60,9 @@ struct StepGraph {
     int64_t k_bodies = 0;    // capture tally of all conditional bodies
 };
 
-// Multigrid hierarchy (defined in mg.h).
+// Multigrid hierarchy (defined in mg.h), learned-guess network (learn.h).
 struct MGHier;
+struct GuessNet;
 
 struct Handle {
     eqc_options opt{};
@@ -115,6 +116,7 @@ struct Handle {
     DBuf<float> g32;      // initial-guess increment added to d before the first solve of a step
     // multigrid
     MGHier* mg = nullptr;     // owned; released by mg_destroy
+    GuessNet* net = nullptr;  // owned; created on first use of the learned-guess entry points
     bool initialized = false;
     // results (main.jl:154-163) gathered on the host
     struct Results {

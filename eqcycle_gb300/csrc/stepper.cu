@@ -9,6 +9,7 @@
 // (dtevol!, src/dtevol.jl:5-44).  Output triggers (main.jl:361-436) are evaluated on the
 // host from the control block.
 #include "model.h"
+#include "learn.h"
 #include "fault.cuh"
 #include "reduce.cuh"
 #include <cmath>
@@ -500,8 +501,15 @@ static void enqueue_qs(Handle& h, bool graph) {
     k_qs_begin<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.F.Vf0.p, h.F.Vf.p, h.F.Nf, h.ctrl.p);
     launch_check();
     count_launch();
+    // learned guess for the first solve (a trained network), and/or logging of training pairs
+    const bool learned = !extrap && h.opt.guess == EQC_GUESS_LEARNED && h.net && h.net->trained;
+    const bool logging = h.net && h.net->log_cap > 0;
+    if (learned || logging) gn_enqueue_features(h);
+    if (learned) gn_enqueue_guess(h);
     for (int p1 = 0; p1 < 2; ++p1) {
-        enqueue_solve(h, h.opt.cg_tol, h.opt.cg_maxit, graph, true, (p1 == 0 && extrap) ? h.g32.p : nullptr);
+        enqueue_solve(h, h.opt.cg_tol, h.opt.cg_maxit, graph, true,
+                      (p1 == 0 && (extrap || learned)) ? h.g32.p : nullptr);
+        if (p1 == 0 && logging) gn_enqueue_log(h);
         apply_K<double>(h.d.p, h.tmp64b.p, args64(h), 1.0, 3, s);  // (K d)[iFlt]
         k_qs_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.tmp64b.p, h.v.p, h.d.p, h.dPre.p, f, h.ctrl.p, p1 == 0);
         launch_check();

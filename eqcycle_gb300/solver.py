@@ -176,6 +176,57 @@ class Solver:
     def set_state(self, name: str, value: np.ndarray):
         self._chk(L.lib().eqc_set_state(self.h, name.encode(), L.dptr(_c(value, np.float64))))
 
+    # -- learned initial guess
+    def guess_shape(self):
+        nin, nout, npar = C.c_int32(0), C.c_int32(0), C.c_int64(0)
+        self._chk(L.lib().eqc_guess_shape(self.h, C.byref(nin), C.byref(nout), C.byref(npar)))
+        return nin.value, nout.value, npar.value
+
+    def guess_init(self, seed: int):
+        self._chk(L.lib().eqc_guess_init(self.h, int(seed)))
+
+    def guess_params(self) -> np.ndarray:
+        p = np.zeros(self.guess_shape()[2], dtype=np.float32)
+        self._chk(L.lib().eqc_guess_get_params(self.h, L.fptr(p)))
+        return p
+
+    def set_guess_params(self, p: np.ndarray):
+        p = _c(p, np.float32)
+        self._chk(L.lib().eqc_guess_set_params(self.h, L.fptr(p)))
+
+    def guess_log(self, capacity: int):
+        self._chk(L.lib().eqc_guess_log(self.h, int(capacity)))
+
+    def guess_pairs(self):
+        nin, nout, _ = self.guess_shape()
+        n = C.c_int64(0)
+        self._chk(L.lib().eqc_guess_pairs(self.h, None, None, C.byref(n)))
+        xin = np.zeros((n.value, nin), dtype=np.float32)
+        tgt = np.zeros((n.value, nout), dtype=np.float32)
+        self._chk(L.lib().eqc_guess_pairs(self.h, L.fptr(xin), L.fptr(tgt), C.byref(n)))
+        return xin, tgt
+
+    def guess_train(self, xin, tgt, epochs: int = 20, lr: float = 1e-3, batch: int = 256, seed: int = 0):
+        xin, tgt = _c(xin, np.float32), _c(tgt, np.float32)
+        loss = np.zeros(epochs)
+        self._chk(L.lib().eqc_guess_train(self.h, L.fptr(xin), L.fptr(tgt), len(xin), epochs, lr, batch, int(seed),
+                                          L.dptr(loss)))
+        return loss
+
+    def guess_eval(self, xin, tgt, outputs: bool = False):
+        xin, tgt = _c(xin, np.float32), _c(tgt, np.float32)
+        mse = C.c_double(0)
+        out = np.zeros(tgt.shape, dtype=np.float32) if outputs else None
+        self._chk(L.lib().eqc_guess_eval(self.h, L.fptr(xin), L.fptr(tgt), len(xin), C.byref(mse), L.fptr(out)))
+        return (mse.value, out) if outputs else mse.value
+
+    def guess_grad(self, xin, tgt):
+        xin, tgt = _c(xin, np.float32), _c(tgt, np.float32)
+        g = np.zeros(self.guess_shape()[2], dtype=np.float32)
+        loss = C.c_double(0)
+        self._chk(L.lib().eqc_guess_grad(self.h, L.fptr(xin), L.fptr(tgt), len(xin), L.fptr(g), C.byref(loss)))
+        return g, loss.value
+
     def scalar(self, name: str) -> float:
         out = C.c_double(0)
         self._chk(L.lib().eqc_get_scalar(self.h, name.encode(), C.byref(out)))

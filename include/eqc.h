@@ -153,6 +153,38 @@ eqc_status eqc_dtevol_noalloc(const double* Vf, const double* XiLf, int64_t n, i
                               double dt, double dtmin, int32_t isolver, double* dt_out,
                               void* stream);
 
+/* ---- learned initial guess -------------------------------------------------------
+ * No counterpart in the reference (src/main.jl:241 always starts CG from the previous
+ * displacement).  A network maps the fault slip increment and slip-rate profile of the
+ * first solve of a quasi-static step ([2][FltNglob] features) to the displacement
+ * increment on a 121 x 61 grid over the domain ([61][121] outputs, depth fastest), which is
+ * prolonged bilinearly to the nodes and added to the previous displacement.  It is used
+ * when the handle was created with guess = EQC_GUESS_LEARNED and the network has been
+ * trained (eqc_guess_train) or given weights (eqc_guess_set_params); CG always runs to the
+ * same tolerance, so the guess changes iteration counts, never the converged result.
+ * Pairs are logged by eqc_run when logging is on (eqc_guess_log). */
+
+/* Feature count (2*FltNglob), output count (121*61) and parameter count of the network. */
+eqc_status eqc_guess_shape(eqc_handle* h, int32_t* nin, int32_t* nout, int64_t* nparam);
+/* Re-initialise the network with seeded He-uniform weights (untrained). */
+eqc_status eqc_guess_init(eqc_handle* h, uint64_t seed);
+/* FP32 master parameters [nparam]; set marks the network trained. */
+eqc_status eqc_guess_get_params(eqc_handle* h, float* params);
+eqc_status eqc_guess_set_params(eqc_handle* h, const float* params);
+/* Log up to `capacity` training pairs during eqc_run (0 switches logging off). */
+eqc_status eqc_guess_log(eqc_handle* h, int64_t capacity);
+/* Logged pairs: *n gets their count; in [n][2][FltNglob] and tgt [n][61][121] (either may be NULL). */
+eqc_status eqc_guess_pairs(eqc_handle* h, float* in, float* tgt, int64_t* n);
+/* Adam training (FP32 master, BF16 weights in every product) on n pairs (in, tgt), or on the
+ * first n pairs this handle logged when both are NULL; epoch_loss[epochs] (optional) gets the
+ * mean squared error per output of every epoch. */
+eqc_status eqc_guess_train(eqc_handle* h, const float* in, const float* tgt, int64_t n, int32_t epochs, double lr,
+                           int32_t batch, uint64_t seed, double* epoch_loss);
+/* Mean squared error per output on n pairs; out [n][61][121] (optional) gets the outputs. */
+eqc_status eqc_guess_eval(eqc_handle* h, const float* in, const float* tgt, int64_t n, double* mse, float* out);
+/* Gradient of that error over one batch of n pairs with respect to every parameter (no update). */
+eqc_status eqc_guess_grad(eqc_handle* h, const float* in, const float* tgt, int64_t n, float* grad, double* loss);
+
 /* ---- the time loop (src/main.jl:67-477) ------------------------------------- */
 
 /* Initial state of main.jl:89-190 with v = V_init/2 (main.jl:102 uses

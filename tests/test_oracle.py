@@ -90,3 +90,45 @@ def test_time_loop_first_steps(oracle_mod):
     dt = np.diff(np.concatenate([[0.0], t]))
     assert np.all(dt[1:] <= 1.2 * dt[:-1] * (1 + 1e-12))   # dtevol: growth capped at 1.2x
     assert np.all(np.isfinite(o.state("d"))) and np.all(np.isfinite(o.state("psi")))
+
+
+def test_guessnet_restatement_gradient_by_finite_differences():
+    """The CPU restatement of the learned-guess network: its backward pass agrees with central
+    differences of its forward pass (FP64 weights, so the check is not hidden by rounding)."""
+    from oracle import guessnet as gn
+    Nf = 13
+    _, _, offs, n = gn.shapes(Nf)
+    rng = np.random.default_rng(0)
+    p = rng.uniform(-0.3, 0.3, n).astype(np.float64)
+    x0 = rng.uniform(-1, 1, (2, 2 * Nf))
+    tgt = rng.uniform(-1, 1, (2, gn.GX * gn.GY))
+    loss, g, _ = gn.loss_and_grad(p, x0, tgt, round_bf16=False)
+    h = 1e-6
+    for name, (o, shp) in offs.items():
+        for j in rng.choice(int(np.prod(shp)), size=3, replace=False):
+            q = p.copy(); q[o + j] += h
+            lp = gn.loss_and_grad(q, x0, tgt, round_bf16=False)[0]
+            q[o + j] -= 2 * h
+            lm = gn.loss_and_grad(q, x0, tgt, round_bf16=False)[0]
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - g[o + j]) <= 1e-6 * max(1.0, abs(fd)) + 1e-9, (name, j, fd, g[o + j])
+
+
+def test_bf16_rounding_restatement():
+    """Round-to-nearest-even to BF16 on known values (ties, carries into the exponent)."""
+    from oracle import guessnet as gn
+    x = np.array([1.0, 1.00390625, 1.005859375, 1.0078125, -2.5, 3.3e-3], dtype=np.float32)
+    # 1 + 2^-8 is a tie between 1 and 1 + 2^-7 -> even (1.0); 1 + 1.5*2^-8 rounds up
+    want = np.array([1.0, 1.0, 1.0078125, 1.0078125, -2.5, 0.0032958984375])
+    assert np.array_equal(gn.bf16(x), want)
+
+
+def test_guessnet_rounds_every_weight_block_and_no_bias():
+    from oracle import guessnet as gn
+    Nf = 13
+    _, _, offs, n = gn.shapes(Nf)
+    p = np.full(n, 0.05, dtype=np.float32)   # 0.05 is not a BF16 value
+    W = gn.unpack(p.astype(np.float64), Nf)
+    for k, v in W.items():
+        want = gn.bf16(np.float32(0.05)) if (k.startswith("cw") or k in ("f1w", "f2w")) else np.float32(0.05)
+        assert np.all(v == np.float64(want)), k
