@@ -314,6 +314,73 @@ def bench_kernel(args):
     print(json.dumps(out), flush=True)
 
 
+def bench_learned(args):
+    """Learned initial guess on the damage-zone model: pairs logged by the plain solver on
+    8 training seeds, Adam on the GPU, evaluated on 2 held-out seeds against the previous-step
+    and the extrapolated guess (same 1e-8 CG tolerance for all)."""
+    from eqcycle_gb300 import (EQC_GUESS_EXTRAPOLATE, EQC_GUESS_LEARNED, EQC_GUESS_PREVIOUS, EQC_MIXED, Solver,
+                               preset, set_parameters)
+    per_seed = max(1, args.pairs // 8)
+    t0 = time.time()
+    xs, ys = [], []
+    for seed in range(1, 9):
+        P = set_parameters(preset(args.workload, seed=seed))
+        with Solver(P, precision=EQC_MIXED, cg_tol=1e-8, guess=EQC_GUESS_PREVIOUS) as s:
+            s.guess_log(per_seed)
+            s.init(P.cfg.V_init)
+            s.set_scalar("dt", steady_dt(s, P))
+            s.run(per_seed)
+            x, y = s.guess_pairs()
+        xs.append(x)
+        ys.append(y)
+    xin, tgt = np.concatenate(xs), np.concatenate(ys)
+    t_log = time.time() - t0
+    held = []
+    params = None
+    report = {"metric": "learned initial guess", "workload": args.workload, "pairs": int(len(xin)),
+              "train_seeds": list(range(1, 9)), "heldout_seeds": [9, 10], "log_s": t_log}
+    for seed in (9, 10):
+        P = set_parameters(preset(args.workload, seed=seed))
+        res = {}
+        for name, mode in (("previous", EQC_GUESS_PREVIOUS), ("extrapolate", EQC_GUESS_EXTRAPOLATE),
+                           ("learned", EQC_GUESS_LEARNED)):
+            with Solver(P, precision=EQC_MIXED, cg_tol=1e-8, guess=mode) as s:
+                if mode == EQC_GUESS_LEARNED:
+                    if params is None:
+                        s.guess_init(0)
+                        t1 = time.time()
+                        losses = s.guess_train(xin, tgt, epochs=args.epochs, lr=1e-3, batch=256, seed=0)
+                        report["train_s"] = time.time() - t1
+                        report["train_loss"] = [float(v) for v in losses]
+                        params = s.guess_params()
+                    else:
+                        s.set_guess_params(params)
+                if mode == EQC_GUESS_PREVIOUS:
+                    s.guess_log(args.steps + args.warmup)
+                s.init(P.cfg.V_init)
+                s.set_scalar("dt", steady_dt(s, P))
+                s.run(args.warmup)
+                tw = s.scalar("t")
+                st = s.run(args.steps)
+                if mode == EQC_GUESS_PREVIOUS:
+                    hx, hy = s.guess_pairs()
+                    held.append((hx, hy))
+                res[name] = {"guess_kept": s.scalar("guess_kept"), "guess_tried": s.scalar("guess_tried"),
+                             "qs_step_ms": st["gpu_ms"] / max(st["qs_steps"], 1),
+                             "cg_iters_per_solve": st["cg_iters"] / max(st["qs_solves"], 1),
+                             "sim_years_per_hr": (st["t"] - tw) / YR / (st["gpu_ms"] / 3.6e6) if st["gpu_ms"] else None}
+        report[f"seed{seed}"] = res
+    # held-out error of the network against the previous-step guess (which predicts 0)
+    P = set_parameters(preset(args.workload, seed=9))
+    hx = np.concatenate([h[0] for h in held])
+    hy = np.concatenate([h[1] for h in held])
+    with Solver(P, precision=EQC_MIXED) as s:
+        s.set_guess_params(params)
+        report["heldout_mse_network"] = s.guess_eval(hx, hy)
+    report["heldout_mse_previous"] = float(np.mean(hy.astype(np.float64) ** 2))
+    print(json.dumps(report), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -326,11 +393,16 @@ def main():
     ap.add_argument("--kernel-only", action="store_true", help="time the stiffness apply alone")
     ap.add_argument("--dtype", default="both", choices=["both", "f32", "f64"])
     ap.add_argument("--nrep", type=int, default=20)
+    ap.add_argument("--learned", action="store_true", help="learned initial guess: train and evaluate")
+    ap.add_argument("--pairs", type=int, default=2400, help="--learned: training pairs over 8 seeds")
+    ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--apply-variant", type=int, default=0,
                     help="stiffness apply kernel: 0 persistent TMA pipeline, 1 one tile per CTA, 2 plain loads")
     args = ap.parse_args()
     if args.kernel_only:
         bench_kernel(args)
+    elif args.learned:
+        bench_learned(args)
     elif args.impl == "reference":
         bench_reference(args)
     else:

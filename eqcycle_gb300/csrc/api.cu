@@ -427,12 +427,14 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         else if (s == "dt") *out = C.dt;
         else if (s == "isolver") *out = C.isolver;
         else if (s == "it") *out = (double)C.it;
-        else if (s == "cg_iters" || s == "qs_solves" || s == "cg_updates" || s == "cg_carried") {
+        else if (s == "cg_iters" || s == "qs_solves" || s == "cg_updates" || s == "cg_carried" ||
+                 s == "guess_tried" || s == "guess_kept") {
             Ctrl c;
             EQC_CUDA(cudaMemcpyAsync(&c, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h.stream));
             EQC_CUDA(cudaStreamSynchronize(h.stream));
             *out = (double)(s == "cg_iters" ? c.cg_iters : s == "qs_solves" ? c.cg_solves
-                            : s == "cg_updates" ? c.cg_updates : c.cg_carried);
+                            : s == "cg_updates" ? c.cg_updates : s == "cg_carried" ? c.cg_carried
+                            : s == "guess_tried" ? c.guess_tried : c.guess_kept);
         }
         else throw Error(EQC_E_ARG, "unknown scalar " + s);
     });

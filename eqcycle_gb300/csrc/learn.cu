@@ -84,6 +84,60 @@ static void gemm(int M, int N, int K, const TA* A, int64_t sam, int64_t sak, con
     count_launch();
 }
 
+// ---- GEMV for small batches (inference): y[b][o] = sum_i x[b][i] W[o][i] + bias[o]; one warp
+// per output row o, lanes striding over i in BF16 pairs; optional GELU copy.
+template <int BMAX>
+__global__ void __launch_bounds__(256) k_gemv(int B, int N, int K, const float* __restrict__ x,
+                                              const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
+                                              float* __restrict__ y, float* __restrict__ yg) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= N) return;
+    const __nv_bfloat16* w = W + (int64_t)warp * K;
+    float acc[BMAX];
+#pragma unroll
+    for (int b = 0; b < BMAX; ++b) acc[b] = 0.f;
+    const bool pairs = ((K & 1) == 0) && ((reinterpret_cast<uintptr_t>(w) & 3) == 0);
+    if (pairs) {
+        const __nv_bfloat162* w2 = reinterpret_cast<const __nv_bfloat162*>(w);
+        for (int i = lane; i < K / 2; i += 32) {
+            const float2 wf = __bfloat1622float2(w2[i]);
+#pragma unroll
+            for (int b = 0; b < BMAX; ++b)
+                if (b < B) acc[b] = fmaf(wf.y, x[(int64_t)b * K + 2 * i + 1], fmaf(wf.x, x[(int64_t)b * K + 2 * i], acc[b]));
+        }
+    } else {
+        for (int i = lane; i < K; i += 32) {
+            const float wf = __bfloat162float(w[i]);
+#pragma unroll
+            for (int b = 0; b < BMAX; ++b)
+                if (b < B) acc[b] = fmaf(wf, x[(int64_t)b * K + i], acc[b]);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < BMAX; ++b) {
+        float v = acc[b];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && b < B) {
+            v += bias ? bias[warp] : 0.f;
+            y[(int64_t)b * N + warp] = v;
+            if (yg) yg[(int64_t)b * N + warp] = gelu(v);
+        }
+    }
+}
+
+// y = x W^T + bias for x [B][K] (FP32), W [N][K] (BF16): GEMV below 5 rows, tiled GEMM above.
+static void linear(int B, int N, int K, const float* x, const __nv_bfloat16* W, const float* bias, float* y, float* yg,
+                   cudaStream_t s) {
+    if (B <= 4) {
+        k_gemv<4><<<(N * 32 + 255) / 256, 256, 0, s>>>(B, N, K, x, W, bias, y, yg);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+    } else {
+        gemm(B, N, K, x, (int64_t)K, (int64_t)1, W, (int64_t)1, (int64_t)K, y, (int64_t)N, bias, yg, s);
+    }
+}
+
 // ---- convolution (kernel 5, stride 2, padding 2) ----------------------------------------
 // z[b][co][t] = bias[co] + sum_{ci,k} W[co][ci][k] in[b][ci][2t+k-2] ; a = GELU(z)
 __global__ void k_conv_fwd(const float* __restrict__ in, int Cin, int Tin, const __nv_bfloat16* __restrict__ W,
@@ -294,10 +348,8 @@ void gn_forward(GuessNet& g, const float* x0, int B, cudaStream_t s) {
         cin = GN_C;
     }
     // fc1: zf1 = a3 W1^T + b1, af1 = GELU(zf1) ; fc2: out = af1 W2^T + b2
-    gemm(B, GN_NH, g.flat, g.a[GN_LAYERS - 1].p, g.flat, 1, g.wbf.p + g.off_f1w, 1, g.flat, g.zf1.p, GN_NH,
-         g.master.p + g.off_f1b, g.af1.p, s);
-    gemm(B, g.nout, GN_NH, g.af1.p, GN_NH, 1, g.wbf.p + g.off_f2w, 1, GN_NH, g.out.p, g.nout, g.master.p + g.off_f2b,
-         (float*)nullptr, s);
+    linear(B, GN_NH, g.flat, g.a[GN_LAYERS - 1].p, g.wbf.p + g.off_f1w, g.master.p + g.off_f1b, g.zf1.p, g.af1.p, s);
+    linear(B, g.nout, GN_NH, g.af1.p, g.wbf.p + g.off_f2w, g.master.p + g.off_f2b, g.out.p, nullptr, s);
 }
 
 // Gradient of the mean squared error of g.out (after gn_forward on x0) against tgt.

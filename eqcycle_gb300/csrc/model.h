@@ -30,6 +30,7 @@ struct Ctrl {
     long long cg_solves;   // solves
     long long cg_updates;  // reliable updates (mixed precision)
     long long cg_carried;  // solves that started from the carried residual
+    long long guess_tried, guess_kept;   // initial-guess increments judged / kept
     int cg_fail;           // bit 0: a solve reached maxit; bit 1: non-finite residual
     int cg_last_it;        // iterations of the last solve
     double cg_last_relres; // ||r|| / ||b|| of the last solve
@@ -46,6 +47,8 @@ struct CGState {
     int it, maxit;
     int done;          // 0 running, 1 converged, 2 maxit reached, 3 non-finite residual
     int need_update;   // mixed precision: a reliable update is due
+    double rr_guess;   // ||r||^2 with the initial-guess increment applied
+    int guess_keep;    // the increment lowered the residual and is kept
 };
 
 // A captured time step (one per regime) and the kernels it launches.

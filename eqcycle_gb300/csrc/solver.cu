@@ -244,9 +244,9 @@ __global__ void __launch_bounds__(VEC_THREADS) k_carry_rows(double* __restrict__
 }
 
 // Carried residual after the guess increment g: r32 -= K_II g (t = K_II g in FP32),
-// S_RR = ||r32||^2.
+// S->rr_guess = ||r32||^2 (S->rr keeps the residual without the increment).
 __global__ void __launch_bounds__(VEC_THREADS) k_guess_residual(float* __restrict__ r32, const float* __restrict__ t,
-                                                                int64_t n, double* part, unsigned* count, double* S) {
+                                                                int64_t n, double* part, unsigned* count, CGState* S) {
     __shared__ double sh[32];
     DotAcc<float> acc;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
@@ -261,7 +261,26 @@ __global__ void __launch_bounds__(VEC_THREADS) k_guess_residual(float* __restric
         st4(r32 + i, rr);
     }
     const double s = block_sum(acc.value(), sh);
-    finish_reduction(s, part, count, sh, [&](double tt2) { S[S_RR] = tt2; });
+    finish_reduction(s, part, count, sh, [&](double tt2) { S->rr_guess = tt2; });
+}
+
+// The previous-step guess judges the increment: keep it only if it lowered ||r||.
+__global__ void k_guess_decide(CGState* S, Ctrl* C) {
+    const int keep = S->rr_guess < S->rr ? 1 : 0;
+    S->guess_keep = keep;
+    if (keep) S->rr = S->rr_guess;
+    C->guess_tried += 1;
+    C->guess_kept += keep;
+}
+// Rejected increment: d -= g, r32 = (float) r64 (the residual without it).
+__global__ void __launch_bounds__(VEC_THREADS) k_guess_revert(const CGState* S, double* __restrict__ d,
+                                                              const float* __restrict__ g, float* __restrict__ r32,
+                                                              const double* __restrict__ r64, int64_t n) {
+    if (S->guess_keep) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        d[i] -= (double)g[i];
+        r32[i] = (float)r64[i];
+    }
 }
 
 // Chooses the residual set-up of a solve: carry (r_valid) or a full FP64 apply.
@@ -340,9 +359,12 @@ static void setup_residual_carry(Handle& h, const float* guess) {
     if (guess) {
         apply_K<float>(guess, h.q32.p, args32(h), 1.0f, 1, h.stream);
         k_guess_residual<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r32.p + ld, h.q32.p + ld, n, h.red_part.p,
-                                                                h.red_count.p, &h.cg.p->rho);
+                                                                h.red_count.p, h.cg.p);
+        k_guess_decide<<<1, 1, 0, h.stream>>>(h.cg.p, h.ctrl.p);
+        k_guess_revert<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.cg.p, h.d.p + ld, guess + ld, h.r32.p + ld,
+                                                              h.r64.p + ld, n);
         EQC_CHECK_LAUNCH();
-        count_launch();
+        count_launch(3);
     }
 }
 
