@@ -124,9 +124,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def run_window(P, precision, W, K, device):
+def run_window(P, precision, W, K, device, params=None, **kw):
     from eqcycle_gb300 import Solver
-    s = Solver(P, precision=precision, cg_tol=1e-8, device=device)
+    s = Solver(P, precision=precision, cg_tol=1e-8, device=device, **kw)
+    if params is not None:
+        s.set_guess_params(params)
     s.init(P.cfg.V_init)
     s.set_scalar("dt", steady_dt(s, P))
     if W:
@@ -180,13 +182,25 @@ def bench_ours(args):
     # ---- plain FP64 method on the window
     s64, st64, sy64, _ = run_window(P, EQC_FP64, args.warmup, args.steps, device)
     s64.close()
-    # ---- headline: mixed precision; state at the window start kept for the e2e leg
-    from eqcycle_gb300 import Solver
-    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device)
+
+    def leg(st_, sy_, s_=None):
+        d = {"value": sy_ / (st_["gpu_ms"] / 3.6e6) if st_["gpu_ms"] else None,
+             "qs_step_ms": st_["gpu_ms"] / max(st_["qs_steps"], 1),
+             "cg_iters_per_solve": st_["cg_iters"] / max(st_["qs_solves"], 1)}
+        if s_ is not None:
+            d["guess_kept"], d["guess_tried"] = s_.scalar("guess_kept"), s_.scalar("guess_tried")
+        return d
+    # ---- headline: mixed precision with the extrapolated guess and the autotuned smoother;
+    # state at the window start kept for the e2e leg
+    from eqcycle_gb300 import Solver, EQC_GUESS_EXTRAPOLATE
+    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device, guess=EQC_GUESS_EXTRAPOLATE)
     s.init(P.cfg.V_init)
     s.set_scalar("dt", steady_dt(s, P))
     if args.warmup:
         s.run(args.warmup)
+    t_tune = time.time()
+    tuned = s.autotune(reps=2)   # after the warm-up: trial solves of a representative step
+    tuned["wall_s"] = time.time() - t_tune
     start = {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}
     t_start, dt_start, iso_start = s.scalar("t"), s.scalar("dt"), s.scalar("isolver")
     clocks = Clocks(device)
@@ -227,6 +241,37 @@ def bench_ours(args):
     if os.path.exists(tp):
         traffic = json.load(open(tp)).get("fp32_bytes_per_launch")
     s.close()
+    # ---- the same window with the previous-step guess (the reference's), and with the learned
+    # guess trained on pairs the plain solver logs on 8 other seeds of the workload
+    from eqcycle_gb300 import EQC_GUESS_LEARNED, EQC_GUESS_PREVIOUS
+    deg = dict(mg_degree=tuned["mg_degree"], mg_degree_coarse=tuned["mg_degree_coarse"])
+    sp, stp, syp, _ = run_window(P, EQC_MIXED, args.warmup, args.steps, device, guess=EQC_GUESS_PREVIOUS, **deg)
+    sp.close()
+    learned = None
+    if args.learned_pairs > 0:
+        t_l = time.time()
+        per_seed = max(1, args.learned_pairs // 8)
+        xs, ys = [], []
+        for seed in range(1, 9):
+            Ps = set_parameters(preset(args.workload, seed=seed))
+            with Solver(Ps, precision=EQC_MIXED, cg_tol=1e-8, device=device, **deg) as sl:
+                sl.guess_log(per_seed)
+                sl.init(Ps.cfg.V_init)
+                sl.set_scalar("dt", steady_dt(sl, Ps))
+                sl.run(per_seed)
+                x, y = sl.guess_pairs()
+            xs.append(x)
+            ys.append(y)
+        with Solver(P, precision=EQC_MIXED, device=device) as st_:
+            st_.guess_init(0)
+            st_.guess_train(np.concatenate(xs), np.concatenate(ys), epochs=20, lr=1e-3, batch=256, seed=0)
+            params = st_.guess_params()
+        sl_, stl, syl, _ = run_window(P, EQC_MIXED, args.warmup, args.steps, device, params=params,
+                                      guess=EQC_GUESS_LEARNED, **deg)
+        learned = leg(stl, syl, sl_)
+        learned["pairs"] = int(sum(len(x) for x in xs))
+        learned["train_and_log_s"] = time.time() - t_l
+        sl_.close()
     if rank != 0:
         return
     line = {
@@ -236,13 +281,16 @@ def bench_ours(args):
         "data": "synthetic: seeded initial state of the damage-zone model (no dataset)",
         "config": {"workload": f"{args.workload}: 480x240-element damage-zone model, 1,846,081 nodes, 961 fault "
                                f"nodes; interseismic window after {args.warmup} warm-up steps from the steady-sliding "
-                               f"start; mixed-precision multigrid-PCG (tol 1e-8)",
+                               f"start; mixed-precision multigrid-PCG (tol 1e-8), extrapolated initial guess, "
+                               f"autotuned smoother",
                    "nodes": nglob, "fault_nodes": Nf, "parallelism": f"replicas x{ws}",
                    "l2": "stiffness-apply roofline timed with an L2 flush between launches"},
         "qs_step_ms": 1e3 * dev_s / max(st["qs_steps"], 1), "cg_iters_per_solve": st["cg_iters"] / max(st["qs_solves"], 1),
         "sim_years_in_window": sim_years,
-        "plain_fp64": {"value": sy64 / (st64["gpu_ms"] / 3.6e6), "qs_step_ms": st64["gpu_ms"] / max(st64["qs_steps"], 1),
-                       "cg_iters_per_solve": st64["cg_iters"] / max(st64["qs_solves"], 1)},
+        "plain_fp64": leg(st64, sy64),
+        "mixed_previous_guess": leg(stp, syp),
+        "learned_mixed": learned,
+        "autotune": tuned,
         "e2e": {"value": e2e_value, "unit": "sim-years/hr", "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps},
         "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -395,6 +443,8 @@ def main():
     ap.add_argument("--nrep", type=int, default=20)
     ap.add_argument("--learned", action="store_true", help="learned initial guess: train and evaluate")
     ap.add_argument("--pairs", type=int, default=2400, help="--learned: training pairs over 8 seeds")
+    ap.add_argument("--learned-pairs", type=int, default=480,
+                    help="training pairs (8 seeds) for the learned-guess leg of the default run (0: skip)")
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--apply-variant", type=int, default=0,
                     help="stiffness apply kernel: 0 persistent TMA pipeline, 1 one tile per CTA, 2 plain loads")

@@ -47,7 +47,7 @@ class EqcOptions(C.Structure):
                 ("cg_tol", C.c_double), ("cg_maxit", C.c_int32), ("device", C.c_int32),
                 ("use_graphs", C.c_int32), ("verbose", C.c_int32),
                 ("reliable_delta", C.c_double), ("mg_degree", C.c_int32), ("mg_coarse_max", C.c_int32),
-                ("mg_cluster_max", C.c_int32), ("apply_variant", C.c_int32)]
+                ("mg_cluster_max", C.c_int32), ("apply_variant", C.c_int32), ("mg_degree_coarse", C.c_int32)]
 
 
 class EqcRunStats(C.Structure):
@@ -67,7 +67,7 @@ EXPORTS = ["eqc_default_options", "eqc_create", "eqc_destroy", "eqc_last_error",
            "eqc_get_scalar", "eqc_set_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
            "eqc_time_apply", "eqc_launch_count", "eqc_sync", "eqc_guess_shape", "eqc_guess_init",
            "eqc_guess_get_params", "eqc_guess_set_params", "eqc_guess_log", "eqc_guess_pairs", "eqc_guess_train",
-           "eqc_guess_eval", "eqc_guess_grad"]
+           "eqc_guess_eval", "eqc_guess_grad", "eqc_autotune"]
 
 
 def lib() -> C.CDLL:
@@ -117,6 +117,7 @@ def lib() -> C.CDLL:
     L.eqc_guess_train.argtypes = [P, _fp, _fp, I64, I32, D, I32, U64, _dp]
     L.eqc_guess_eval.argtypes = [P, _fp, _fp, I64, _dp, _fp]
     L.eqc_guess_grad.argtypes = [P, _fp, _fp, I64, _fp, _dp]
+    L.eqc_autotune.argtypes = [P, I32, C.POINTER(I32), C.POINTER(I32), _dp]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L

@@ -265,7 +265,8 @@ static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x) {
     if (with_x) level_apply<T>(h, l, x, t);
     k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)(1.0 / theta), with_x ? 1 : 0);
     count_launch();
-    for (int k = 1; k < m.deg; ++k) {
+    const int deg = (l == 0) ? m.deg : m.deg_coarse;
+    for (int k = 1; k < deg; ++k) {
         level_apply<T>(h, l, d, t);
         const double rho_new = 1.0 / (2.0 * sigma - rho);
         k_cheb_step<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, t, Dinv, n, (T)(rho_new * rho), (T)(2.0 * rho_new / delta));
@@ -419,11 +420,15 @@ static void setup_cluster_cycle(Handle& h) {
     int first = -1;
     for (int l = 1; l <= L; ++l)
         if ((int64_t)m.lev[l - 1].cx * m.lev[l - 1].cy <= cl_max) { first = l; break; }
-    if (cl_max < 0 || first < 0 || L - first > CL_MAXLEV || m.deg > CL_MAXDEG) { m.cl_first = -1; m.cl_size = 0; return; }
+    if (cl_max < 0 || first < 0 || L - first > CL_MAXLEV || m.deg_coarse > CL_MAXDEG) {
+        m.cl_first = -1;
+        m.cl_size = 0;
+        return;
+    }
     const int cs = cluster_setup<T>();
     if (cs == 0) { m.cl_first = -1; m.cl_size = 0; return; }
     P.nlev = L - first;
-    P.deg = m.deg;
+    P.deg = m.deg_coarse;
     for (int l = first; l < L; ++l) {
         StencilLevel& S = m.lev[l - 1];
         MGWork& w = m.work[l];
@@ -442,7 +447,7 @@ static void setup_cluster_cycle(Handle& h) {
         const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
         double rho = 1.0 / sigma;
         c.inv_theta = (T)(1.0 / theta);
-        for (int k = 1; k < m.deg; ++k) {   // the same recurrence as chebyshev()
+        for (int k = 1; k < m.deg_coarse; ++k) {   // the same recurrence as chebyshev()
             const double rho_new = 1.0 / (2.0 * sigma - rho);
             c.c1[k] = (T)(rho_new * rho);
             c.c2[k] = (T)(2.0 * rho_new / delta);
@@ -503,6 +508,7 @@ void mg_build(Handle& h) {
     // coarser vertex grids
     const int64_t coarse_max = h.opt.mg_coarse_max > 0 ? h.opt.mg_coarse_max : 2048;
     if (h.opt.mg_degree > 0) m.deg = h.opt.mg_degree;
+    m.deg_coarse = h.opt.mg_degree_coarse > 0 ? h.opt.mg_degree_coarse : 3;
     while ((int64_t)m.lev.back().cx * (m.lev.back().cy - 1) > coarse_max && m.lev.back().cx >= 5 &&
            m.lev.back().cy >= 5) {
         StencilLevel& f = m.lev.back();

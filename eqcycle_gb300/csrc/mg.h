@@ -79,7 +79,8 @@ template <class T> int cluster_setup();   // cluster size usable on this device 
 template <class T> void cluster_cycle(const ClusterArgs<T>& P, int cluster, cudaStream_t s);
 
 struct MGHier {
-    int deg = 4;
+    int deg = 4;          // Chebyshev steps on the spectral-element level
+    int deg_coarse = 3;   // ... on the vertex levels
     double lo_ratio = 30.0;
     double lmax0 = 0;
     double gll_lo[4] = {0, 0, 0, 0}, gll_hi[4] = {0, 0, 0, 0};   // SEM <-> vertex weights

@@ -47,6 +47,9 @@ struct CGState {
     int it, maxit;
     int done;          // 0 running, 1 converged, 2 maxit reached, 3 non-finite residual
     int need_update;   // mixed precision: a reliable update is due
+    double sigma;      // mixed precision: the FP32 recurrence vectors hold sigma * (true value),
+                       // sigma a power of two near 1 / ||b|| (keeps tiny residuals out of
+                       // FP32 underflow); 1 in FP64.  rr is in those scaled units.
     double rr_guess;   // ||r||^2 with the initial-guess increment applied
     int guess_keep;    // the increment lowered the residual and is kept
 };

@@ -102,24 +102,27 @@ __global__ void k_jacobi(const T* __restrict__ r, const T* __restrict__ dg, T* _
         z[i] = r[i] / dg[i];
 }
 
-// x64 += (double) y32 ; y32 = 0
-__global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, float* __restrict__ y, int64_t n) {
+// x64 += (double) y32 / sigma ; y32 = 0   (sigma a power of two: the division is exact)
+__global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, float* __restrict__ y, int64_t n,
+                                                      const CGState* S) {
+    const double inv = 1.0 / S->sigma;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double xx[4];
         float yy[4];
         ld4(x + i, xx);
         ld4(y + i, yy);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) xx[k] += (double)yy[k];
+        for (int k = 0; k < 4; ++k) xx[k] += (double)yy[k] * inv;
         st4(x + i, xx);
         const float zero[4] = {0.f, 0.f, 0.f, 0.f};
         st4(y + i, zero);
     }
 }
-// r32 = (float) r64 ; S_RR = r64.r64
+// r32 = (float) (sigma r64) ; S->rr = sigma^2 r64.r64
 __global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(const double* __restrict__ r64, float* __restrict__ r32,
-                                                             int64_t n, double* part, unsigned* count, double* S) {
+                                                             int64_t n, double* part, unsigned* count, CGState* S) {
     __shared__ double sh[32];
+    const double sg = S->sigma;
     double s = 0.0;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double v[4];
@@ -127,13 +130,20 @@ __global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(const double* __res
         ld4(r64 + i, v);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            f[k] = (float)v[k];
+            f[k] = (float)(v[k] * sg);
             s += v[k] * v[k];
         }
         st4(r32 + i, f);
     }
     s = block_sum(s, sh);
-    finish_reduction(s, part, count, sh, [&](double t) { S[S_RR] = t; });
+    finish_reduction(s, part, count, sh, [&](double t) { S->rr = t * sg * sg; });
+}
+
+// Scale of the FP32 recurrence for this solve: sigma = 2^-e with 2^e <= ||b|| < 2^(e+1)
+// (1 in FP64, or when b = 0).
+__global__ void k_set_sigma(CGState* S, int mixed) {
+    const double nb = sqrt(S->bb);
+    S->sigma = (mixed && nb > 0 && isfinite(nb)) ? ldexp(1.0, -ilogb(nb)) : 1.0;
 }
 
 static inline dim3 vgrid() { return dim3(VEC_BLOCKS); }
@@ -144,7 +154,7 @@ static inline dim3 vgrid() { return dim3(VEC_BLOCKS); }
 
 // Start of a solve: S->bb, S->rr hold ||b||^2 and ||r0||^2.
 __global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, cudaGraphConditionalHandle hw, int use_cond) {
-    const double nb = sqrt(S->bb), r = sqrt(S->rr);
+    const double nb = sqrt(S->bb), r = sqrt(S->rr) / S->sigma;
     const double reltol = (rule == EQC_TOL_R0 ? r : nb) * tol;
     S->nb = nb;
     S->reltol = reltol;
@@ -163,7 +173,7 @@ __global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, cudaGraph
 // End of an FP64 iteration: the loop goes on until ||r|| <= reltol or maxit.
 __global__ void k_cg_check(CGState* S, cudaGraphConditionalHandle hw, int use_cond) {
     S->it += 1;
-    const double r = sqrt(S->rr);
+    const double r = sqrt(S->rr) / S->sigma;
     S->res = r;
     const int st = !isfinite(r) ? 3 : (r <= S->reltol ? 1 : (S->it >= S->maxit ? 2 : 0));
     S->done = st;
@@ -174,7 +184,7 @@ __global__ void k_cg_check(CGState* S, cudaGraphConditionalHandle hw, int use_co
 // (the recurrence residual fell by `delta` since the last one, or the loop would stop).
 __global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandle hi, int use_cond) {
     S->it += 1;
-    const double rs = sqrt(S->rr);
+    const double rs = sqrt(S->rr) / S->sigma;
     int need = 0;
     if (!isfinite(rs)) {
         S->done = 3;
@@ -192,7 +202,7 @@ __global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandl
 __global__ void k_cg_check_b(CGState* S, Ctrl* C, cudaGraphConditionalHandle hw, int use_cond) {
     if (S->done != 3) {
         if (S->need_update) {
-            const double rs = sqrt(S->rr);
+            const double rs = sqrt(S->rr) / S->sigma;
             S->res = rs;
             S->rmax = rs;
             S->need_update = 0;
@@ -226,28 +236,18 @@ __global__ void k_fault_delta(const double* __restrict__ d, double* __restrict__
     }
 }
 
-// Carried residual, rows 1..4 (the only rows K_IF reaches): r64 += t, r32 = (float) r64,
-// S_RR += sum(r_new^2 - r_old^2).
-__global__ void __launch_bounds__(VEC_THREADS) k_carry_rows(double* __restrict__ r64, float* __restrict__ r32,
-                                                            const double* __restrict__ t, int64_t n, double* part,
-                                                            unsigned* count, double* S) {
-    __shared__ double sh[32];
-    double s = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double ro = r64[i], rn = ro + t[i];
-        r64[i] = rn;
-        r32[i] = (float)rn;
-        s += rn * rn - ro * ro;
-    }
-    s = block_sum(s, sh);
-    finish_reduction(s, part, count, sh, [&](double tt) { S[S_RR] += tt; });
+// Carried residual, rows 1..4 (the only rows K_IF reaches): r64 += t.
+__global__ void k_carry_rows(double* __restrict__ r64, const double* __restrict__ t, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r64[i] += t[i];
 }
 
-// Carried residual after the guess increment g: r32 -= K_II g (t = K_II g in FP32),
+// Carried residual after the guess increment g: r32 -= sigma K_II g (t = K_II g in FP32),
 // S->rr_guess = ||r32||^2 (S->rr keeps the residual without the increment).
 __global__ void __launch_bounds__(VEC_THREADS) k_guess_residual(float* __restrict__ r32, const float* __restrict__ t,
                                                                 int64_t n, double* part, unsigned* count, CGState* S) {
     __shared__ double sh[32];
+    const float sg = (float)S->sigma;
     DotAcc<float> acc;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         float rr[4], tt[4];
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(VEC_THREADS) k_guess_residual(float* __restric
         ld4(t + i, tt);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            rr[k] -= tt[k];
+            rr[k] -= sg * tt[k];
             acc.add(rr[k], rr[k]);
         }
         st4(r32 + i, rr);
@@ -272,14 +272,15 @@ __global__ void k_guess_decide(CGState* S, Ctrl* C) {
     C->guess_tried += 1;
     C->guess_kept += keep;
 }
-// Rejected increment: d -= g, r32 = (float) r64 (the residual without it).
+// Rejected increment: d -= g, r32 = (float) (sigma r64) (the residual without it).
 __global__ void __launch_bounds__(VEC_THREADS) k_guess_revert(const CGState* S, double* __restrict__ d,
                                                               const float* __restrict__ g, float* __restrict__ r32,
                                                               const double* __restrict__ r64, int64_t n) {
     if (S->guess_keep) return;
+    const double sg = S->sigma;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         d[i] -= (double)g[i];
-        r32[i] = (float)r64[i];
+        r32[i] = (float)(r64[i] * sg);
     }
 }
 
@@ -324,10 +325,13 @@ void precond<float>(Handle& h, const float* r, float* z, int64_t n) {
 }
 
 // Right-hand side: S->bb = ||b||^2 with b = -K_IF F on rows 1..4 (d holds F on row 0).
-static void setup_rhs(Handle& h) {
+static void setup_rhs(Handle& h, bool mixed) {
     const int64_t ld = h.L.ld;
     apply_K<double>(h.d.p, h.tmp64a.p, args64(h), -1.0, 2, h.stream);
     dot64(h, h.tmp64a.p + ld, h.tmp64a.p + ld, 4 * ld, &h.cg.p->bb);
+    k_set_sigma<<<1, 1, 0, h.stream>>>(h.cg.p, mixed ? 1 : 0);
+    EQC_CHECK_LAUNCH();
+    count_launch();
 }
 
 // Full initial residual: r64 = b - K_II d_I (rows >= 1, row 0 zero), S->rr = ||r||^2, and in
@@ -339,7 +343,7 @@ static void setup_residual_full(Handle& h, bool mixed) {
     apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);     // r = -(K d)_I
     if (mixed) {
         k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p,
-                                                             h.red_count.p, &S->rho);
+                                                             h.red_count.p, S);
         EQC_CHECK_LAUNCH();
         count_launch();
     } else {
@@ -347,15 +351,17 @@ static void setup_residual_full(Handle& h, bool mixed) {
     }
 }
 
-// Carried residual: r64 -= K_IF (F - Flast) on rows 1..4 (tmp64b row 0 holds F - Flast), and
-// with a guess increment g in d: r32 -= K_II g (the first reliable update recomputes r64).
+// Carried residual: r64 -= K_IF (F - Flast) on rows 1..4 (tmp64b row 0 holds F - Flast), then
+// r32 = sigma r64 for this solve's sigma; with a guess increment g in d: r32 -= sigma K_II g
+// (the first reliable update recomputes r64).
 static void setup_residual_carry(Handle& h, const float* guess) {
     const int64_t ld = h.L.ld, n = h.L.size() - ld;
     apply_K<double>(h.tmp64b.p, h.tmp64c.p, args64(h), -1.0, 2, h.stream);
-    k_carry_rows<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, h.tmp64c.p + ld, 4 * ld,
-                                                        h.red_part.p, h.red_count.p, &h.cg.p->rho);
+    k_carry_rows<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.tmp64c.p + ld, 4 * ld);
+    k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p,
+                                                         h.red_count.p, h.cg.p);
     EQC_CHECK_LAUNCH();
-    count_launch();
+    count_launch(2);
     if (guess) {
         apply_K<float>(guess, h.q32.p, args32(h), 1.0f, 1, h.stream);
         k_guess_residual<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r32.p + ld, h.q32.p + ld, n, h.red_part.p,
@@ -417,10 +423,10 @@ static void update_mixed(Handle& h) {
     const Layout& L = h.L;
     const int64_t ld = L.ld, n = L.size() - ld;
     CGState* S = h.cg.p;
-    k_fold<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.d.p + ld, h.x32.p + ld, n);
+    k_fold<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.d.p + ld, h.x32.p + ld, n, S);
     apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);
     k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p, h.red_count.p,
-                                                         &S->rho);
+                                                         S);
     EQC_CHECK_LAUNCH();
     count_launch(2);
 }
@@ -436,7 +442,7 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry, con
     const bool mixed = h.opt.precision == EQC_MIXED;
     carry = carry && mixed;
     const double delta = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : RELIABLE_DELTA;
-    setup_rhs(h);
+    setup_rhs(h, mixed);
     if (carry) {
         k_fault_delta<<<(h.F.Nf + 255) / 256, 256, 0, h.stream>>>(h.d.p, h.F.Flast.p, h.tmp64b.p, h.F.Nf);
         EQC_CHECK_LAUNCH();

@@ -57,7 +57,7 @@ class Solver:
                  guess: int = L.EQC_GUESS_PREVIOUS, cg_tol: float = 1e-8, cg_maxit: int = 0,
                  tol_rule: int = L.EQC_TOL_RHS, device: int = 0, use_graphs: int = 1, verbose: int = 0,
                  reliable_delta: float = 0.0, mg_degree: int = 0, mg_coarse_max: int = 0,
-                 mg_cluster_max: int = 0, apply_variant: int = 0):
+                 mg_cluster_max: int = 0, apply_variant: int = 0, mg_degree_coarse: int = 0):
         self.P = P
         lib = L.lib()
         fa, ia, m = P.farray, P.iarray, P.mesh
@@ -91,7 +91,8 @@ class Solver:
                                          cg_maxit=cg_maxit, tol_rule=tol_rule, device=device,
                                          use_graphs=use_graphs, verbose=verbose, reliable_delta=reliable_delta,
                                          mg_degree=mg_degree, mg_coarse_max=mg_coarse_max,
-                                         mg_cluster_max=mg_cluster_max, apply_variant=apply_variant)
+                                         mg_cluster_max=mg_cluster_max, apply_variant=apply_variant,
+                                         mg_degree_coarse=mg_degree_coarse)
         h = C.c_void_p()
         L.check(lib.eqc_create(C.byref(mod), C.byref(self.options), C.byref(h)), None)
         self.h = h
@@ -175,6 +176,12 @@ class Solver:
 
     def set_state(self, name: str, value: np.ndarray):
         self._chk(L.lib().eqc_set_state(self.h, name.encode(), L.dptr(_c(value, np.float64))))
+
+    def autotune(self, reps: int = 2):
+        """Choose the multigrid smoothing degrees by timed trial solves (state unchanged)."""
+        dg, dc, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
+        self._chk(L.lib().eqc_autotune(self.h, reps, C.byref(dg), C.byref(dc), C.byref(ms)))
+        return {"mg_degree": dg.value, "mg_degree_coarse": dc.value, "solve_ms": ms.value}
 
     # -- learned initial guess
     def guess_shape(self):

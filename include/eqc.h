@@ -88,12 +88,14 @@ typedef struct {
     /* solver tuning (0 = default) */
     double reliable_delta;  /* mixed precision: FP64 residual replacement whenever the
                                recurrence residual fell by this factor (default 1e-3)  */
-    int32_t mg_degree;      /* Chebyshev smoothing steps per level, pre and post (default 4) */
+    int32_t mg_degree;      /* Chebyshev smoothing steps on the spectral-element level, pre and
+                               post (default 4)                                        */
     int32_t mg_coarse_max;  /* largest coarsest level, solved densely (default 2048 unknowns) */
     int32_t mg_cluster_max; /* > 0: levels with at most this many grid points run as one
                                thread-block-cluster launch (default 0: off)            */
     int32_t apply_variant;  /* stiffness apply kernel: 0 persistent TMA pipeline (default),
                                1 one tile per CTA by TMA, 2 plain loads                */
+    int32_t mg_degree_coarse; /* Chebyshev steps on the vertex levels (default 3)          */
 } eqc_options;
 
 typedef struct eqc_handle eqc_handle;
@@ -241,6 +243,13 @@ eqc_status eqc_apply_K_device(eqc_handle* h, const void* x, void* y, int32_t dty
  * stream, flushing L2 between launches when flush_l2 != 0; *ms gets the mean
  * launch duration. */
 eqc_status eqc_time_apply(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t flush_l2, double* ms);
+
+/* Solver autotuner (no counterpart in the reference): times `reps` graph-replayed trial
+ * solves of the next quasi-static solve from the current state for a set of Chebyshev
+ * degrees (spectral-element level x vertex levels) and keeps the fastest; the state and the
+ * counters are restored.  *mg_degree, *mg_degree_coarse and *solve_ms (all optional) get the
+ * choice and its trial time.  Call after eqc_init (or between eqc_run calls). */
+eqc_status eqc_autotune(eqc_handle* h, int32_t reps, int32_t* mg_degree, int32_t* mg_degree_coarse, double* solve_ms);
 
 /* Kernel launches of the library since the handle was created. */
 int64_t eqc_launch_count(eqc_handle* h);

@@ -204,3 +204,46 @@ def test_mixed_time_loop_matches_fp64_oracle(eqclib, oracle_mod, guess):
     assert carried >= st["qs_solves"] - 2     # every solve but the first carries
     for k in ("d", "v", "psi", "tau"):
         assert rel(got[k], o.state(k)) <= 1e-6, k
+
+
+def test_autotune_keeps_the_state_and_chooses_a_valid_smoother(eqclib):
+    """eqc_autotune leaves the state and the counters untouched; the run after it converges to
+    the same state as a run with the default smoother (same CG tolerance)."""
+    cfg = preset("dz40")
+    P = set_parameters(cfg)
+    out = []
+    for tune in (False, True):
+        with Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG, guess=2, cg_tol=1e-10) as s:
+            s.init(cfg.V_init)
+            s.run(3)   # past the trivial first solves of the steady start
+            if tune:
+                before = {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}
+                scal = {k: s.scalar(k) for k in ("t", "dt", "isolver", "cg_iters", "qs_solves")}
+                res = s.autotune(reps=1)
+                assert res["mg_degree"] in (3, 4, 5) and res["mg_degree_coarse"] in (1, 3, 4)
+                assert res["solve_ms"] > 0
+                for k, v in before.items():
+                    assert np.array_equal(s.state(k), v), k
+                for k, v in scal.items():
+                    assert s.scalar(k) == v, k
+            st = s.run(8)
+            assert st["qs_steps"] == 8
+            out.append({k: s.state(k) for k in ("d", "v", "psi")})
+    for k in out[0]:
+        assert rel(out[1][k], out[0][k]) <= 1e-6, k
+
+
+def test_mixed_precision_from_the_steady_start(eqclib):
+    """From V = Vpl the first increments are ~1e-25 m: the FP32 recurrence works on scaled
+    vectors (no underflow) and tracks the FP64 method."""
+    cfg = preset("dz40")
+    P = set_parameters(cfg)
+    res = {}
+    for prec in (EQC_FP64, EQC_MIXED):
+        with Solver(P, precision=prec, precond=EQC_PC_AMG, cg_tol=1e-10) as s:
+            s.init(cfg.V_init)
+            st = s.run(12)
+            assert st["qs_steps"] == 12
+            res[prec] = {k: s.state(k) for k in ("d", "v", "psi")}
+    for k in res[EQC_FP64]:
+        assert rel(res[EQC_MIXED][k], res[EQC_FP64][k]) <= 1e-6, k
