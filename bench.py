@@ -447,7 +447,8 @@ def main():
                     help="training pairs (8 seeds) for the learned-guess leg of the default run (0: skip)")
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--apply-variant", type=int, default=0,
-                    help="stiffness apply kernel: 0 persistent TMA pipeline, 1 one tile per CTA, 2 plain loads")
+                    help="stiffness apply kernel: 0 default, 1 one tile per CTA (TMA), 2 plain tile loads, "
+                         "3 persistent TMA pipeline")
     args = ap.parse_args()
     if args.kernel_only:
         bench_kernel(args)

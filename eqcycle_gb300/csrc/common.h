@@ -111,7 +111,7 @@ struct ApplyArgs {
     const T* Wp;      // [WPad*Nel] padded copy for TMA (may be null)
     int* err;         // device flag set when a bounded wait gives up (may be null)
     TmaCache* tma;    // host-side tensor-map cache (may be null)
-    int variant;      // 0 persistent TMA pipeline, 1 one tile per CTA by TMA, 2 plain loads
+    int variant;      // see eqc_options.apply_variant
 };
 
 // Error text for entry points without a handle (returned by eqc_last_error(NULL)).

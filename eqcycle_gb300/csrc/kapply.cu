@@ -14,6 +14,7 @@
 // and 5 y-lines (sum factorisation: two 5x5 contractions per line) staged through
 // shared memory.
 #include "model.h"
+#include "vec.cuh"
 #include <cstdlib>
 #include <algorithm>
 
@@ -454,6 +455,142 @@ __global__ void __launch_bounds__(NT) k_apply_pipe(const __grid_constant__ CUten
     }
 }
 
+// ---- element-per-lane version (FP32) --------------------------------------------------------
+// One lane per element, one warp per element row of 31 elements plus a halo lane (lane 0 = the
+// element left of the strip), RW_ROWS element rows per CTA plus a halo warp (warp 0 = the row
+// below the group).  Every lane contracts its element's 5 x-lines and 5 y-lines in registers
+// (no W merging across elements): the 4 x 4 nodes it owns (local i, j < 4) are complete once the
+// right-column contributions of the left lane (shuffle) and the top-row contributions of the warp
+// below (shared memory, one barrier) are added.  Node rows arrive as 16-byte loads (the 5th node
+// of a row is the next lane's first), element data as seven 16-byte loads of the padded W copy.
+// The last node row and column are owned by a virtual element row / column with W = 0.
+constexpr int RW_ROWS = 8;
+constexpr unsigned FULLMASK = 0xffffffffu;
+
+template <int MINB>
+__global__ void __launch_bounds__(32 * (RW_ROWS + 1), MINB) k_apply_rows(const float* __restrict__ x, float* __restrict__ y,
+                                                                        ApplyArgs<float> A, float sign, int zero_row0) {
+    const Layout L = A.L;
+    __shared__ float Ts[RW_ROWS + 1][5][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int ex = (int)blockIdx.x * 31 - 1 + lane;
+    const int ey = (int)blockIdx.y * RW_ROWS - 1 + w;
+    const bool real = ex >= 0 && ex < L.NelX && ey >= 0 && ey < L.NelY;
+
+    // every load of the lane is issued before the first use (one memory latency, not twelve)
+    float4 v[5];
+    float n4s[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        const int iy = 4 * ey + j;
+        const bool rowok = iy >= 0 && iy < L.ny;
+        v[j] = (rowok && ex >= 0 && 4 * ex < L.nx) ? __ldg(reinterpret_cast<const float4*>(x + (int64_t)iy * L.ld + 4 * ex))
+                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int ix = 4 * ex + 4;
+        n4s[j] = (lane == 31 && rowok && ix >= 0 && ix < L.nx) ? __ldg(x + (int64_t)iy * L.ld + ix) : 0.f;
+    }
+    float4 wq[7];
+    const float4* wp = reinterpret_cast<const float4*>(A.Wp + ((int64_t)(real ? ey : 0) * L.NelX + (real ? ex : 0)) * 28);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) wq[k] = real ? __ldg(wp + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+    float u[5][5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        u[j][0] = v[j].x;
+        u[j][1] = v[j].y;
+        u[j][2] = v[j].z;
+        u[j][3] = v[j].w;
+        const float n4 = __shfl_down_sync(FULLMASK, v[j].x, 1);
+        u[j][4] = lane == 31 ? n4s[j] : n4;
+    }
+    float W[28];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        W[4 * k] = wq[k].x;
+        W[4 * k + 1] = wq[k].y;
+        W[4 * k + 2] = wq[k].z;
+        W[4 * k + 3] = wq[k].w;
+    }
+
+    float out[4][4], R[4], T[5];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) out[j][i] = 0.f;
+    // x-lines (the halo warp needs only the top one)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        if (w == 0 && j < 4) continue;
+        float sp[5];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc += Hc<float>(k, p) * u[j][k];
+            sp[p] = W[p + 5 * j] * acc;
+        }
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            float acc = 0.f;
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += Hc<float>(i, p) * sp[p];
+            const float o = A.c1 * acc;
+            if (j < 4) {
+                if (i < 4) out[j][i] = o;
+                else R[j] = o;
+            } else {
+                T[i] = o;
+            }
+        }
+    }
+    // y-lines
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        float sp[5];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            float acc = 0.f;
+#pragma unroll
+            for (int l = 0; l < 5; ++l) acc += u[l][i] * Hc<float>(l, p);
+            sp[p] = W[i + 5 * p] * acc;
+        }
+#pragma unroll
+        for (int jj = 0; jj < 5; ++jj) {
+            float acc = 0.f;
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += sp[p] * Hc<float>(jj, p);
+            const float o = A.c2 * acc;
+            if (jj < 4) {
+                if (i < 4) out[jj][i] += o;
+                else R[jj] += o;
+            } else {
+                T[i] += o;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) Ts[w][i][lane] = T[i];
+    float Rl[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) Rl[j] = __shfl_up_sync(FULLMASK, R[j], 1);
+    __syncthreads();
+    if (w == 0 || lane == 0 || ex > L.NelX || ey > L.NelY) return;
+    // contributions of the left element (right column) and of the element row below (top row)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) out[j][0] += Rl[j];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) out[0][i] += Ts[w - 1][i][lane];
+    out[0][0] += Ts[w - 1][4][lane - 1];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int iy = 4 * ey + j;
+        if (iy >= L.ny) break;
+        const float z = (zero_row0 && iy == 0) ? 0.f : sign;
+        *reinterpret_cast<float4*>(y + (int64_t)iy * L.ld + 4 * ex) =
+            make_float4(z * out[j][0], z * out[j][1], z * out[j][2], z * out[j][3]);
+    }
+}
+
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                      const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                      CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -567,6 +704,16 @@ template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s) {
     if (mode <= 1) {
         dim3 grid(A.L.NelX / LTEX + 1, A.L.NelY / LTEY + 1);
+        if constexpr (sizeof(T) == 4) {
+            if ((A.variant == 0 || A.variant == 4) && A.Wp && aligned16(x) && aligned16(y)) {
+                dim3 g((A.L.NelX + 1 + 30) / 31, (A.L.NelY + 1 + RW_ROWS - 1) / RW_ROWS);
+                if (A.variant == 4) k_apply_rows<3><<<g, 32 * (RW_ROWS + 1), 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
+                else k_apply_rows<2><<<g, 32 * (RW_ROWS + 1), 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
+                EQC_CHECK_LAUNCH();
+                count_launch();
+                return;
+            }
+        }
         const CUtensorMap* um = (A.tma && A.variant != 2) ? tma_umap<T>(*A.tma, x, A.L) : nullptr;
         if (um && A.variant == 1) {
             k_apply_tma<T, LTEX, LTEY, LNT><<<grid, LNT, 0, s>>>(*um, tma_wmap<T>(*A.tma), y, A, sign, mode == 1 ? 1 : 0);

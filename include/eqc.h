@@ -93,8 +93,9 @@ typedef struct {
     int32_t mg_coarse_max;  /* largest coarsest level, solved densely (default 2048 unknowns) */
     int32_t mg_cluster_max; /* > 0: levels with at most this many grid points run as one
                                thread-block-cluster launch (default 0: off)            */
-    int32_t apply_variant;  /* stiffness apply kernel: 0 persistent TMA pipeline (default),
-                               1 one tile per CTA by TMA, 2 plain loads                */
+    int32_t apply_variant;  /* stiffness apply kernel: 0 default (FP32: one element per lane,
+                               FP64: persistent TMA pipeline), 1 one tile per CTA by
+                               TMA, 2 plain tile loads, 3 persistent TMA pipeline     */
     int32_t mg_degree_coarse; /* Chebyshev steps on the vertex levels (default 3)          */
 } eqc_options;
 
