@@ -16,6 +16,7 @@
 #include "model.h"
 #include "vec.cuh"
 #include <cstdlib>
+#include <type_traits>
 #include <algorithm>
 
 namespace eqc {
@@ -457,24 +458,91 @@ __global__ void __launch_bounds__(NT) k_apply_pipe(const __grid_constant__ CUten
 
 // ---- element-per-lane version (FP32) --------------------------------------------------------
 // One lane per element, one warp per element row of 31 elements plus a halo lane (lane 0 = the
-// element left of the strip), RW_ROWS element rows per CTA plus a halo warp (warp 0 = the row
+// element left of the strip), ROWS element rows per CTA plus a halo warp (warp 0 = the row
 // below the group).  Every lane contracts its element's 5 x-lines and 5 y-lines in registers
 // (no W merging across elements): the 4 x 4 nodes it owns (local i, j < 4) are complete once the
 // right-column contributions of the left lane (shuffle) and the top-row contributions of the warp
 // below (shared memory, one barrier) are added.  Node rows arrive as 16-byte loads (the 5th node
 // of a row is the next lane's first), element data as seven 16-byte loads of the padded W copy.
 // The last node row and column are owned by a virtual element row / column with W = 0.
-constexpr int RW_ROWS = 8;
 constexpr unsigned FULLMASK = 0xffffffffu;
 
-template <int MINB>
-__global__ void __launch_bounds__(32 * (RW_ROWS + 1), MINB) k_apply_rows(const float* __restrict__ x, float* __restrict__ y,
-                                                                        ApplyArgs<float> A, float sign, int zero_row0) {
+// The 5 x-lines and 5 y-lines of one element (u: its 5 x 5 nodes, W: its 25 weights): the owned
+// outputs out[j][i] (i, j < 4), the right column R[j] (j < 4) and the top row T[i] (i <= 4).
+// top_only: only T is needed (the halo row).
+template <class WAcc>
+__device__ __forceinline__ void rows_lines_t(const float (&u)[5][5], const WAcc& W, float c1, float c2,
+                                           bool top_only, float (&out)[4][4], float (&R)[4], float (&T)[5]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) out[j][i] = 0.f;
+    // x-lines (the halo warp needs only the top one)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        if (top_only && j < 4) continue;
+        float sp[5];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc += Hc<float>(k, p) * u[j][k];
+            sp[p] = W[p + 5 * j] * acc;
+        }
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            float acc = 0.f;
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += Hc<float>(i, p) * sp[p];
+            const float o = c1 * acc;
+            if (j < 4) {
+                if (i < 4) out[j][i] = o;
+                else R[j] = o;
+            } else {
+                T[i] = o;
+            }
+        }
+    }
+    // y-lines
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        float sp[5];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            float acc = 0.f;
+#pragma unroll
+            for (int l = 0; l < 5; ++l) acc += u[l][i] * Hc<float>(l, p);
+            sp[p] = W[i + 5 * p] * acc;
+        }
+#pragma unroll
+        for (int jj = 0; jj < 5; ++jj) {
+            float acc = 0.f;
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc += sp[p] * Hc<float>(jj, p);
+            const float o = c2 * acc;
+            if (jj < 4) {
+                if (i < 4) out[jj][i] += o;
+                else R[jj] += o;
+            } else {
+                T[i] += o;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void rows_lines(const float (&u)[5][5], const float (&W)[28], float c1, float c2,
+                                           bool top_only, float (&out)[4][4], float (&R)[4], float (&T)[5]) {
+    rows_lines_t(u, W, c1, c2, top_only, out, R, T);
+}
+
+template <int ROWS, int MINB>
+__global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const float* __restrict__ x, float* __restrict__ y,
+                                                                     ApplyArgs<float> A, float sign, int zero_row0) {
     const Layout L = A.L;
-    __shared__ float Ts[RW_ROWS + 1][5][32];
+    __shared__ float Ts[ROWS + 1][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int ex = (int)blockIdx.x * 31 - 1 + lane;
-    const int ey = (int)blockIdx.y * RW_ROWS - 1 + w;
+    const int ey = (int)blockIdx.y * ROWS - 1 + w;
     const bool real = ex >= 0 && ex < L.NelX && ey >= 0 && ey < L.NelY;
 
     // every load of the lane is issued before the first use (one memory latency, not twelve)
@@ -513,61 +581,7 @@ __global__ void __launch_bounds__(32 * (RW_ROWS + 1), MINB) k_apply_rows(const f
     }
 
     float out[4][4], R[4], T[5];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) out[j][i] = 0.f;
-    // x-lines (the halo warp needs only the top one)
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        if (w == 0 && j < 4) continue;
-        float sp[5];
-#pragma unroll
-        for (int p = 0; p < 5; ++p) {
-            float acc = 0.f;
-#pragma unroll
-            for (int k = 0; k < 5; ++k) acc += Hc<float>(k, p) * u[j][k];
-            sp[p] = W[p + 5 * j] * acc;
-        }
-#pragma unroll
-        for (int i = 0; i < 5; ++i) {
-            float acc = 0.f;
-#pragma unroll
-            for (int p = 0; p < 5; ++p) acc += Hc<float>(i, p) * sp[p];
-            const float o = A.c1 * acc;
-            if (j < 4) {
-                if (i < 4) out[j][i] = o;
-                else R[j] = o;
-            } else {
-                T[i] = o;
-            }
-        }
-    }
-    // y-lines
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        float sp[5];
-#pragma unroll
-        for (int p = 0; p < 5; ++p) {
-            float acc = 0.f;
-#pragma unroll
-            for (int l = 0; l < 5; ++l) acc += u[l][i] * Hc<float>(l, p);
-            sp[p] = W[i + 5 * p] * acc;
-        }
-#pragma unroll
-        for (int jj = 0; jj < 5; ++jj) {
-            float acc = 0.f;
-#pragma unroll
-            for (int p = 0; p < 5; ++p) acc += sp[p] * Hc<float>(jj, p);
-            const float o = A.c2 * acc;
-            if (jj < 4) {
-                if (i < 4) out[jj][i] += o;
-                else R[jj] += o;
-            } else {
-                T[i] += o;
-            }
-        }
-    }
+    rows_lines(u, W, A.c1, A.c2, w == 0, out, R, T);
 #pragma unroll
     for (int i = 0; i < 5; ++i) Ts[w][i][lane] = T[i];
     float Rl[4];
@@ -698,6 +712,28 @@ void set_H(const double* H, cudaStream_t s) {
                                   (int)apply_smem<float>()));
     pipe_setup<float>();
     pipe_setup<double>();
+
+}
+
+// Element-per-lane apply: variant 0 -> 6 element rows per CTA (default), 4..7 -> 4, 6, 8, 12.
+static void launch_rows(const float* x, float* y, const ApplyArgs<float>& A, float sign, int zr, cudaStream_t s) {
+    const int sx = (A.L.NelX + 1 + 30) / 31;
+    auto go = [&](auto rows_tag, auto minb_tag) {
+        constexpr int R = decltype(rows_tag)::value, M = decltype(minb_tag)::value;
+        dim3 g(sx, (A.L.NelY + 1 + R - 1) / R);
+        k_apply_rows<R, M><<<g, 32 * (R + 1), 0, s>>>(x, y, A, sign, zr);
+    };
+    using I = std::integral_constant<int, 0>;
+    (void)sizeof(I);
+    switch (A.variant) {
+        case 4: go(std::integral_constant<int, 4>{}, std::integral_constant<int, 3>{}); break;
+        case 5: go(std::integral_constant<int, 8>{}, std::integral_constant<int, 2>{}); break;
+        case 6: go(std::integral_constant<int, 12>{}, std::integral_constant<int, 1>{}); break;
+        case 7: go(std::integral_constant<int, 6>{}, std::integral_constant<int, 2>{}); break;
+        default: go(std::integral_constant<int, 6>{}, std::integral_constant<int, 3>{}); break;
+    }
+    EQC_CHECK_LAUNCH();
+    count_launch();
 }
 
 template <class T>
@@ -705,12 +741,8 @@ void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStre
     if (mode <= 1) {
         dim3 grid(A.L.NelX / LTEX + 1, A.L.NelY / LTEY + 1);
         if constexpr (sizeof(T) == 4) {
-            if ((A.variant == 0 || A.variant == 4) && A.Wp && aligned16(x) && aligned16(y)) {
-                dim3 g((A.L.NelX + 1 + 30) / 31, (A.L.NelY + 1 + RW_ROWS - 1) / RW_ROWS);
-                if (A.variant == 4) k_apply_rows<3><<<g, 32 * (RW_ROWS + 1), 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
-                else k_apply_rows<2><<<g, 32 * (RW_ROWS + 1), 0, s>>>(x, y, A, sign, mode == 1 ? 1 : 0);
-                EQC_CHECK_LAUNCH();
-                count_launch();
+            if ((A.variant == 0 || A.variant >= 4) && A.Wp && aligned16(x) && aligned16(y)) {
+                launch_rows(x, y, A, sign, mode == 1 ? 1 : 0, s);
                 return;
             }
         }
