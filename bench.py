@@ -193,7 +193,8 @@ def bench_ours(args):
     # ---- headline: mixed precision with the extrapolated guess and the autotuned smoother;
     # state at the window start kept for the e2e leg
     from eqcycle_gb300 import Solver, EQC_GUESS_EXTRAPOLATE
-    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device, guess=EQC_GUESS_EXTRAPOLATE)
+    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device, guess=EQC_GUESS_EXTRAPOLATE,
+               use_graphs=0 if args.no_graphs else 1)
     s.init(P.cfg.V_init)
     s.set_scalar("dt", steady_dt(s, P))
     if args.warmup:
@@ -295,7 +296,7 @@ def bench_ours(args):
                 "d2h_bytes_per_step": d2h / args.steps},
         "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": bytes32 / (ms32 * 1e-3) / 1e9 / peak, "traffic": traffic,
-                     "kernel": "k_apply<float> (FP32 stiffness apply)", "peak_kind": peak_kind,
+                     "kernel": "k_apply_rows<6,3> (FP32 stiffness apply, one element per lane)", "peak_kind": peak_kind,
                      "launch_us": ms32 * 1e3, "algorithmic_bytes": bytes32},
         "fp64_apply": {"launch_us": ms64 * 1e3, "algorithmic_bytes": bytes64,
                        "achieved_gbs": bytes64 / (ms64 * 1e-3) / 1e9},
@@ -442,6 +443,8 @@ def main():
     ap.add_argument("--dtype", default="both", choices=["both", "f32", "f64"])
     ap.add_argument("--nrep", type=int, default=20)
     ap.add_argument("--learned", action="store_true", help="learned initial guess: train and evaluate")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="headline leg without CUDA graphs (host-driven steps; for per-kernel profiling)")
     ap.add_argument("--pairs", type=int, default=2400, help="--learned: training pairs over 8 seeds")
     ap.add_argument("--learned-pairs", type=int, default=480,
                     help="training pairs (8 seeds) for the learned-guess leg of the default run (0: skip)")

@@ -159,15 +159,28 @@ __global__ void k_sub(const T* __restrict__ b, const T* __restrict__ t, T* __res
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         r[i] = b[i] - t[i];
 }
-// x[cx + k] = sum_j Cinv[k][j] b[cx + j]  (one warp per row)
+// x[cx + k] = sum_j Cinv[k][j] b[cx + j]  (one warp per row).  Accumulates in T: FP32 for the
+// FP32 cycle (a preconditioner; GB300's FP64 rate would make this the slowest kernel of it).
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
 template <class T>
 __global__ void k_dense_mv(const T* __restrict__ Cinv, const T* __restrict__ b, T* __restrict__ x, int n, int off) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= n) return;
-    double s = 0.0;
-    for (int j = lane; j < n; j += 32) s += (double)Cinv[(int64_t)warp * n + j] * (double)b[off + j];
-    s = warp_sum(s);
-    if (lane == 0) x[off + warp] = (T)s;
+    const T* row = Cinv + (int64_t)warp * n;
+    T s0 = T(0), s1 = T(0);
+    int j = lane;
+    for (; j + 32 < n; j += 64) {
+        s0 += row[j] * b[off + j];
+        s1 += row[j + 32] * b[off + j + 32];
+    }
+    if (j < n) s0 += row[j] * b[off + j];
+    const T s = warp_sum_t(s0 + s1);
+    if (lane == 0) x[off + warp] = s;
 }
 template <class T>
 __global__ void k_scale(T* x, int64_t n, double s) {
