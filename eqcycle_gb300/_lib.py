@@ -67,7 +67,8 @@ EXPORTS = ["eqc_default_options", "eqc_create", "eqc_destroy", "eqc_last_error",
            "eqc_get_scalar", "eqc_set_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
            "eqc_time_apply", "eqc_launch_count", "eqc_sync", "eqc_guess_shape", "eqc_guess_init",
            "eqc_guess_get_params", "eqc_guess_set_params", "eqc_guess_log", "eqc_guess_pairs", "eqc_guess_train",
-           "eqc_guess_eval", "eqc_guess_grad", "eqc_autotune"]
+           "eqc_guess_eval", "eqc_guess_grad", "eqc_autotune", "eqc_ensemble_create", "eqc_ensemble_run",
+           "eqc_ensemble_destroy", "eqc_ensemble_last_error"]
 
 
 def lib() -> C.CDLL:
@@ -118,6 +119,11 @@ def lib() -> C.CDLL:
     L.eqc_guess_eval.argtypes = [P, _fp, _fp, I64, _dp, _fp]
     L.eqc_guess_grad.argtypes = [P, _fp, _fp, I64, _fp, _dp]
     L.eqc_autotune.argtypes = [P, I32, C.POINTER(I32), C.POINTER(I32), _dp]
+    L.eqc_ensemble_create.argtypes = [C.POINTER(P), I32, C.POINTER(P)]
+    L.eqc_ensemble_run.argtypes = [P, I64, C.POINTER(EqcRunStats), _dp]
+    L.eqc_ensemble_destroy.argtypes = [P]
+    L.eqc_ensemble_last_error.restype = C.c_char_p
+    L.eqc_ensemble_last_error.argtypes = [P]
     for name in EXPORTS:
         getattr(L, name)
     _lib = L

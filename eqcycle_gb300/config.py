@@ -123,3 +123,29 @@ def preset(name: str, seed: int = 0) -> ModelConfig:
             rho2=2670.0, vs2=0.6 * 3464.0, trap_w0=500.0, trap_w1=200.0, trap_z1=10e3,
             total_years=years, rec_x=rx, rec_y=ry)
     raise ValueError(f"unknown preset {name!r}")
+
+
+def ensemble_members(n: int = 64, seed: int = 0, nmin: int = 120, nmax: int = 480):
+    """The batched-ensemble workload: ``n`` damage-zone fault models with uneven meshes and seeded
+    parameters (one ``ModelConfig`` each).
+
+    Mesh: fault-normal elements N drawn uniformly from multiples of 8 in [nmin, nmax], N/2 along
+    depth (120 x 60 to 480 x 240 elements over the same 48 km x 24 km domain).  Per model, drawn
+    from one seeded stream: damage-zone width uniform in [0, 2] km at the surface (narrowing to 40 %
+    of it at 10 km depth, the shape of the dz presets), vs reduction uniform in [0, 60] %, Dc
+    log-uniform in [4, 16] mm, a - b uniform in [-0.006, -0.002] in the seismogenic zone (a = 0.015,
+    b below 15 km unchanged), and the theta noise seed.
+    """
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        N = int(8 * rng.integers(nmin // 8, nmax // 8 + 1))
+        w = float(rng.uniform(0.0, 2000.0))
+        red = float(rng.uniform(0.0, 0.6))
+        Dc = float(np.exp(rng.uniform(np.log(4e-3), np.log(16e-3))))
+        amb = float(rng.uniform(-0.006, -0.002))
+        cfg = preset(f"dz{N}", seed=1000 + k).replace(
+            trap_w0=w, trap_w1=0.4 * w, vs2=(1.0 - red) * 3464.0, Dc=Dc, b0=0.015 - amb, total_years=500.0)
+        out.append(cfg)
+    return out

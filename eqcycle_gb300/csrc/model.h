@@ -185,6 +185,13 @@ int64_t capture_tally();
 // stepper.cu
 void init_state(Handle& h, double V_init);
 void destroy_graphs(Handle& h);
+// One whole time step of regime iso (1 quasi-static, 2 dynamic) on h.stream; graph: inside a capture.
+void enqueue_step(Handle& h, int iso, bool graph);
+// Host side of a finished step (control block already in h.h_ctrl): checks and outputs.
+struct PostBufs {
+    std::vector<double> dF, vF, tauF, seis;
+};
+void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb);
 void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st);
 void fault_slrFunc(Handle& h, const double* psi, double* psi1, const double* Vf, double* Vf1, const double* tau1,
                    double dt);

@@ -546,7 +546,7 @@ static void enqueue_dyn(Handle& h) {
 }
 
 // One whole time step, ending with the control kernel (Vfmax, regime, next dt).
-static void enqueue_step(Handle& h, int iso, bool graph) {
+void enqueue_step(Handle& h, int iso, bool graph) {
     k_step_begin<<<1, 1, 0, h.stream>>>(h.ctrl.p);
     count_launch();
     if (iso == 1) enqueue_qs(h, graph);
@@ -587,6 +587,112 @@ static StepGraph& step_graph(Handle& h, int iso) {
     return G;
 }
 
+// Host side of one finished step (the control block is in h.h_ctrl): failure checks and the
+// output triggers of main.jl:361-436.
+void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb) {
+    cudaStream_t s = h.stream;
+    const int Nf = h.F.Nf;
+    const double Vpl = h.Vpl;
+    const std::vector<double>& tauo = h.h_tauo;
+    const std::vector<double>& FltX = h.h_FltX;
+    Ctrl& C = *h.h_ctrl;
+    std::vector<double>& dF = pb.dF;
+    std::vector<double>& vF = pb.vF;
+    std::vector<double>& tauF = pb.tauF;
+    std::vector<double>& seis = pb.seis;
+    if (seis.size() < (size_t)(3 * std::max(h.nSeis, 1))) seis.resize(3 * std::max(h.nSeis, 1));
+    if (iso == 1) stats.qs_steps++;
+    else stats.dyn_steps++;
+    const double tnow = C.t;
+    h.res.time_.push_back(tnow);
+    if (C.fail != 0x7fffffff)
+        throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(C.fail));
+    if (C.apply_err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
+    if (C.cg_fail & 2) throw Error(EQC_E_NAN, "non-finite residual in CG");
+    if (C.cg_fail & 1)
+        throw Error(EQC_E_CG, "CG did not converge within maxit (relres " + std::to_string(C.cg_last_relres) + ")");
+    const double Vfmax = C.Vfmax;
+    if (!std::isfinite(Vfmax)) throw Error(EQC_E_NAN, "non-finite slip rate");
+    // ---- outputs (main.jl:361-436) ----
+    bool need_cols = (Vfmax > 1.01 * h.Vthres && h.slipstart == 0) ||
+                     (Vfmax < 0.99 * h.Vthres && h.slipstart == 1) || (tnow > h.tvsx) || (Vfmax > h.Vevne);
+    if (need_cols) fault_columns(h, dF, vF, tauF);
+    auto push_col = [&](std::vector<double>& dst, int which) {
+        for (int k = 0; k < Nf; ++k) {
+            double val;
+            if (which == 0) val = 2 * dF[k] + Vpl * tnow;
+            else if (which == 1) val = 2 * vF[k] + Vpl;
+            else val = (tauF[k] + tauo[k]) / 1e6;
+            dst.push_back(val);
+        }
+    };
+    if (Vfmax > 1.01 * h.Vthres && h.slipstart == 0) {
+        if (h.it_s >= CAP_EV) throw Error(EQC_E_CAPACITY, "event capacity (400) exceeded");
+        h.it_s += 1;
+        for (int k = 0; k < Nf; ++k) h.delfref[k] = 2 * dF[k] + Vpl * tnow;
+        h.slipstart = 1;
+        h.res.tStart.push_back(tnow);
+        push_col(h.res.taubefore, 2);
+        h.res.hypo.push_back(FltX[C.ihypo]);
+    }
+    if (Vfmax < 0.99 * h.Vthres && h.slipstart == 1) {
+        h.it_e += 1;
+        for (int k = 0; k < Nf; ++k) h.res.delfafter.push_back(2 * dF[k] + Vpl * tnow - h.delfref[k]);
+        push_col(h.res.tauafter, 2);
+        h.res.tEnd.push_back(tnow);
+        h.slipstart = 0;
+    }
+    if (tnow > h.tvsx) {
+        if (h.ntvsx >= CAP_IS) throw Error(EQC_E_CAPACITY, "interseismic snapshot capacity (4000) exceeded");
+        h.ntvsx += 1;
+        h.idd += 1;
+        push_col(h.res.is_slip, 0);
+        push_col(h.res.is_slipvel, 1);
+        push_col(h.res.is_stress, 2);
+        h.tvsx = h.tvsx + h.tvsxinc;
+    }
+    if (Vfmax > h.Vevne) {
+        if (h.idelevne == 0) {
+            if (h.nevne >= CAP_SEISMIC) throw Error(EQC_E_CAPACITY, "seismic snapshot capacity exceeded");
+            h.nevne += 1;
+            h.idd += 1;
+            h.idelevne = 1;
+            h.tevneb = tnow;
+            h.tevne = h.tevneinc;
+            push_col(h.res.seismic_slip, 0);
+            push_col(h.res.seismic_slipvel, 1);
+            push_col(h.res.seismic_stress, 2);
+        }
+        if (h.idelevne == 1 && (tnow - h.tevneb) > h.tevne) {
+            if (h.nevne >= CAP_SEISMIC) throw Error(EQC_E_CAPACITY, "seismic snapshot capacity exceeded");
+            h.nevne += 1;
+            h.idd += 1;
+            push_col(h.res.seismic_slip, 0);
+            push_col(h.res.seismic_slipvel, 1);
+            push_col(h.res.seismic_stress, 2);
+            h.tevne = h.tevne + h.tevneinc;
+        }
+    } else {
+        h.idelevne = 0;
+    }
+    if (h.opt.verbose && C.it % 500 == 0) printf("Time (yr) = %1.5g\n", tnow / h.yr2sec);
+    if (C.it % 10 == 0 && h.nSeis > 0) {
+        if (h.rit >= CAP_SEIS) throw Error(EQC_E_CAPACITY, "receiver capacity (190000) exceeded");
+        h.rit += 1;
+        k_gather_seis<<<1, 32, 0, s>>>(h.iSeis.p, h.nSeis, h.d.p, h.v.p, h.a.p, h.seis.p);
+        count_launch();
+        EQC_CUDA(cudaMemcpyAsync(seis.data(), h.seis.p, sizeof(double) * 3 * h.nSeis, cudaMemcpyDeviceToHost, s));
+        EQC_CUDA(cudaStreamSynchronize(s));
+        for (int k = 0; k < h.nSeis; ++k) {
+            h.res.dSeis.push_back(seis[k]);
+            h.res.vSeis.push_back(seis[h.nSeis + k]);
+            h.res.aSeis.push_back(seis[2 * h.nSeis + k]);
+        }
+    }
+    h.res.Vfmax.push_back(Vfmax);
+    stats.steps++;
+}
+
 void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
     if (!h.initialized) throw Error(EQC_E_STATE, "eqc_run before eqc_init");
     cudaStream_t s = h.stream;
@@ -596,7 +702,7 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
     const std::vector<double>& FltX = h.h_FltX;
     auto t0 = std::chrono::steady_clock::now();
     eqc_run_stats stats{};
-    std::vector<double> dF, vF, tauF, seis(3 * std::max(h.nSeis, 1));
+    PostBufs pb;
     Ctrl& C = *h.h_ctrl;
     EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
     EQC_CUDA(cudaStreamSynchronize(s));
@@ -624,96 +730,7 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
             EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
             EQC_CUDA(cudaStreamSynchronize(s));
         }
-        if (iso == 1) stats.qs_steps++;
-        else stats.dyn_steps++;
-        const double tnow = C.t;
-        h.res.time_.push_back(tnow);
-        if (C.fail != 0x7fffffff)
-            throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(C.fail));
-        if (C.apply_err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
-        if (C.cg_fail & 2) throw Error(EQC_E_NAN, "non-finite residual in CG");
-        if (C.cg_fail & 1)
-            throw Error(EQC_E_CG, "CG did not converge within maxit (relres " + std::to_string(C.cg_last_relres) + ")");
-        const double Vfmax = C.Vfmax;
-        if (!std::isfinite(Vfmax)) throw Error(EQC_E_NAN, "non-finite slip rate");
-        // ---- outputs (main.jl:361-436) ----
-        bool need_cols = (Vfmax > 1.01 * h.Vthres && h.slipstart == 0) ||
-                         (Vfmax < 0.99 * h.Vthres && h.slipstart == 1) || (tnow > h.tvsx) || (Vfmax > h.Vevne);
-        if (need_cols) fault_columns(h, dF, vF, tauF);
-        auto push_col = [&](std::vector<double>& dst, int which) {
-            for (int k = 0; k < Nf; ++k) {
-                double val;
-                if (which == 0) val = 2 * dF[k] + Vpl * tnow;
-                else if (which == 1) val = 2 * vF[k] + Vpl;
-                else val = (tauF[k] + tauo[k]) / 1e6;
-                dst.push_back(val);
-            }
-        };
-        if (Vfmax > 1.01 * h.Vthres && h.slipstart == 0) {
-            if (h.it_s >= CAP_EV) throw Error(EQC_E_CAPACITY, "event capacity (400) exceeded");
-            h.it_s += 1;
-            for (int k = 0; k < Nf; ++k) h.delfref[k] = 2 * dF[k] + Vpl * tnow;
-            h.slipstart = 1;
-            h.res.tStart.push_back(tnow);
-            push_col(h.res.taubefore, 2);
-            h.res.hypo.push_back(FltX[C.ihypo]);
-        }
-        if (Vfmax < 0.99 * h.Vthres && h.slipstart == 1) {
-            h.it_e += 1;
-            for (int k = 0; k < Nf; ++k) h.res.delfafter.push_back(2 * dF[k] + Vpl * tnow - h.delfref[k]);
-            push_col(h.res.tauafter, 2);
-            h.res.tEnd.push_back(tnow);
-            h.slipstart = 0;
-        }
-        if (tnow > h.tvsx) {
-            if (h.ntvsx >= CAP_IS) throw Error(EQC_E_CAPACITY, "interseismic snapshot capacity (4000) exceeded");
-            h.ntvsx += 1;
-            h.idd += 1;
-            push_col(h.res.is_slip, 0);
-            push_col(h.res.is_slipvel, 1);
-            push_col(h.res.is_stress, 2);
-            h.tvsx = h.tvsx + h.tvsxinc;
-        }
-        if (Vfmax > h.Vevne) {
-            if (h.idelevne == 0) {
-                if (h.nevne >= CAP_SEISMIC) throw Error(EQC_E_CAPACITY, "seismic snapshot capacity exceeded");
-                h.nevne += 1;
-                h.idd += 1;
-                h.idelevne = 1;
-                h.tevneb = tnow;
-                h.tevne = h.tevneinc;
-                push_col(h.res.seismic_slip, 0);
-                push_col(h.res.seismic_slipvel, 1);
-                push_col(h.res.seismic_stress, 2);
-            }
-            if (h.idelevne == 1 && (tnow - h.tevneb) > h.tevne) {
-                if (h.nevne >= CAP_SEISMIC) throw Error(EQC_E_CAPACITY, "seismic snapshot capacity exceeded");
-                h.nevne += 1;
-                h.idd += 1;
-                push_col(h.res.seismic_slip, 0);
-                push_col(h.res.seismic_slipvel, 1);
-                push_col(h.res.seismic_stress, 2);
-                h.tevne = h.tevne + h.tevneinc;
-            }
-        } else {
-            h.idelevne = 0;
-        }
-        if (h.opt.verbose && C.it % 500 == 0) printf("Time (yr) = %1.5g\n", tnow / h.yr2sec);
-        if (C.it % 10 == 0 && h.nSeis > 0) {
-            if (h.rit >= CAP_SEIS) throw Error(EQC_E_CAPACITY, "receiver capacity (190000) exceeded");
-            h.rit += 1;
-            k_gather_seis<<<1, 32, 0, s>>>(h.iSeis.p, h.nSeis, h.d.p, h.v.p, h.a.p, h.seis.p);
-            count_launch();
-            EQC_CUDA(cudaMemcpyAsync(seis.data(), h.seis.p, sizeof(double) * 3 * h.nSeis, cudaMemcpyDeviceToHost, s));
-            EQC_CUDA(cudaStreamSynchronize(s));
-            for (int k = 0; k < h.nSeis; ++k) {
-                h.res.dSeis.push_back(seis[k]);
-                h.res.vSeis.push_back(seis[h.nSeis + k]);
-                h.res.aSeis.push_back(seis[2 * h.nSeis + k]);
-            }
-        }
-        h.res.Vfmax.push_back(Vfmax);
-        stats.steps++;
+        post_step(h, iso, stats, pb);
     }
     EQC_CUDA(cudaEventRecord(ev1, s));
     EQC_CUDA(cudaEventSynchronize(ev1));

@@ -280,3 +280,44 @@ def main(P: Params, V_init: Optional[float] = None, max_steps: int = 1 << 62, **
         s.init(V_init)
         s.run(max_steps)
         return s.results()
+
+
+class Ensemble:
+    """Independent fault models (``Solver`` objects on one GPU) advanced by one CUDA-graph launch
+    per time step, each member in its own regime (``eqc_ensemble_*``)."""
+
+    def __init__(self, members):
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        h = C.c_void_p()
+        st = L.lib().eqc_ensemble_create(arr, len(self.members), C.byref(h))
+        L.check(st, None)
+        self.h = h
+
+    def run(self, steps: int):
+        """Advance every member by ``steps`` steps; returns ([stats dict per member], gpu_ms)."""
+        n = len(self.members)
+        stats = (L.EqcRunStats * n)()
+        ms = C.c_double(0)
+        st = L.lib().eqc_ensemble_run(self.h, int(steps), stats, C.byref(ms))
+        if st != L.EQC_OK:
+            msg = L.lib().eqc_ensemble_last_error(self.h)
+            raise L.EqcError(st, msg.decode() if msg else "")
+        return [stats[i].as_dict() for i in range(n)], ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().eqc_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

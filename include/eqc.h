@@ -230,6 +230,21 @@ eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);
 int64_t    eqc_result_size(eqc_handle* h, const char* field);
 eqc_status eqc_get_result(eqc_handle* h, const char* field, double* out);
 
+/* ---- ensembles --------------------------------------------------------------------
+ * No counterpart in the reference (it runs one model per process).  An ensemble advances
+ * several independent models (handles created by eqc_create on the same device, initialised
+ * by eqc_init, uneven sizes allowed) by one CUDA-graph launch per time step: each member is a
+ * branch of the graph whose regime (quasi-static or dynamic) is chosen on the device from the
+ * member's own state, and the members run concurrently.  Every member keeps its own results
+ * (eqc_get_result on the member handle); the ensemble does not own the handles. */
+typedef struct eqc_ensemble eqc_ensemble;
+eqc_status eqc_ensemble_create(eqc_handle* const* members, int32_t n, eqc_ensemble** out);
+/* Advance every member by `steps` time steps; stats[n] (optional) gets each member's
+ * statistics, *gpu_ms (optional) the CUDA-event time of the whole call. */
+eqc_status eqc_ensemble_run(eqc_ensemble* e, int64_t steps, eqc_run_stats* stats, double* gpu_ms);
+eqc_status eqc_ensemble_destroy(eqc_ensemble* e);
+const char* eqc_ensemble_last_error(const eqc_ensemble* e);
+
 /* ---- device-resident entry points (benchmarks, integration with device codes) */
 
 /* Internal node layout: lexicographic grid, depth fastest, fault = row 0.

@@ -247,3 +247,37 @@ def test_mixed_precision_from_the_steady_start(eqclib):
             res[prec] = {k: s.state(k) for k in ("d", "v", "psi")}
     for k in res[EQC_FP64]:
         assert rel(res[EQC_MIXED][k], res[EQC_FP64][k]) <= 1e-6, k
+
+
+def test_ensemble_equals_members_run_alone(eqclib):
+    """Uneven models advanced together by one graph launch per step (one of them in the dynamic
+    regime) end bitwise where each ends when run alone."""
+    from eqcycle_gb300 import Ensemble
+    base = preset("homog48")
+    cfgs = [base.replace(NelX=8, NelY=12, LX=4e3, LY=6e3, creep_depth=4e3),
+            SMALL.replace(V_init=2e-2),
+            base.replace(NelX=10, NelY=20, LX=5e3, LY=10e3, creep_depth=5e3, seed=3)]
+    Ps = [set_parameters(c) for c in cfgs]
+    alone = []
+    for c, P in zip(cfgs, Ps):
+        with Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG, guess=2) as s:
+            s.init(c.V_init)
+            st = s.run(12)
+            alone.append((st, {k: s.state(k) for k in ("d", "v", "psi")}, s.results().Vfmax))
+    solvers = [Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG, guess=2) for P in Ps]
+    try:
+        for c, s in zip(cfgs, solvers):
+            s.init(c.V_init)
+        with Ensemble(solvers) as E:
+            stats, ms = E.run(12)
+        assert ms > 0
+        assert any(st["dyn_steps"] > 0 for st in stats) and any(st["qs_steps"] == 12 for st in stats)
+        for (st0, x0, vf0), st, s in zip(alone, stats, solvers):
+            for k in ("steps", "qs_steps", "dyn_steps", "cg_iters"):
+                assert st[k] == st0[k], k
+            for k, v in x0.items():
+                assert np.array_equal(s.state(k), v), k
+            assert np.array_equal(s.results().Vfmax, vf0)
+    finally:
+        for s in solvers:
+            s.close()
