@@ -475,13 +475,54 @@ def bench_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_cycle(args):
+    """Whole earthquake cycles, quasi-static and dynamic phases: the plain FP64 method and the mixed
+    method (extrapolated guess, autotuned smoother) each run the model for --years simulated years
+    (or until --cycle-budget seconds of wall time), then their event catalogues are compared
+    (recurrence interval, coseismic slip, hypocentre depth)."""
+    from eqcycle_gb300 import EQC_FP64, EQC_GUESS_EXTRAPOLATE, EQC_GUESS_PREVIOUS, EQC_MIXED, Solver, preset, \
+        set_parameters
+    from eqcycle_gb300.events import catalogue, compare
+    wl = args.workload or "homog48"
+    cfg = preset(wl)
+    P = set_parameters(cfg)
+    t_end = (args.years or cfg.total_years) * YR
+    mu = cfg.rho1 * cfg.vs1 ** 2
+    out, cats = {}, {}
+    for name, prec, guess in (("plain_fp64", EQC_FP64, EQC_GUESS_PREVIOUS), ("mixed", EQC_MIXED, EQC_GUESS_EXTRAPOLATE)):
+        with Solver(P, precision=prec, cg_tol=1e-8, guess=guess) as s:
+            s.init(cfg.V_init)
+            gpu_ms, qs, dyn, cg, solves, wall0 = 0.0, 0, 0, 0, 0, time.time()
+            tuned = None
+            while s.scalar("t") < t_end and time.time() - wall0 < args.cycle_budget:
+                st = s.run(2000, t_end)
+                gpu_ms += st["gpu_ms"]
+                qs += st["qs_steps"]
+                dyn += st["dyn_steps"]
+                cg += st["cg_iters"]
+                solves += st["qs_solves"]
+                if prec == EQC_MIXED and tuned is None and qs >= 20:
+                    tuned = s.autotune(reps=2)
+            years = s.scalar("t") / YR
+            res = s.results()
+        cat = catalogue(res, P.farray.FltX, mu)
+        cats[name] = cat
+        out[name] = {"sim_years": years, "value": years / (gpu_ms / 3.6e6) if gpu_ms else None,
+                     "gpu_s": gpu_ms / 1e3, "wall_s": time.time() - wall0, "qs_steps": qs, "dyn_steps": dyn,
+                     "cg_iters_per_solve": cg / max(solves, 1), "autotune": tuned, **cat.summary()}
+    line = {"metric": "sim-years/hr over whole cycles", "workload": wl, "years_target": t_end / YR,
+            "plain_fp64": out["plain_fp64"], "mixed": out["mixed"],
+            "event_statistics_mixed_vs_fp64": compare(cats["plain_fp64"], cats["mixed"])}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dz480")
+    ap.add_argument("--workload", default=None, help="dz480 (default), dz960, homog48 (--cycle default), ...")
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true", help="time the stiffness apply alone")
@@ -489,6 +530,9 @@ def main():
     ap.add_argument("--nrep", type=int, default=20)
     ap.add_argument("--learned", action="store_true", help="learned initial guess: train and evaluate")
     ap.add_argument("--ensemble", action="store_true", help="batched ensemble of uneven fault models")
+    ap.add_argument("--cycle", action="store_true", help="whole cycles: sim-years/hr and event statistics")
+    ap.add_argument("--years", type=float, default=0.0, help="--cycle: simulated years (default: the workload's)")
+    ap.add_argument("--cycle-budget", type=float, default=600.0, help="--cycle: wall seconds per method")
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--no-graphs", action="store_true",
                     help="headline leg without CUDA graphs (host-driven steps; for per-kernel profiling)")
@@ -500,12 +544,16 @@ def main():
                     help="stiffness apply kernel: 0 default, 1 one tile per CTA (TMA), 2 plain tile loads, "
                          "3 persistent TMA pipeline")
     args = ap.parse_args()
+    if args.workload is None and not args.cycle:
+        args.workload = "dz480"
     if args.kernel_only:
         bench_kernel(args)
     elif args.learned:
         bench_learned(args)
     elif args.ensemble:
         bench_ensemble(args)
+    elif args.cycle:
+        bench_cycle(args)
     elif args.impl == "reference":
         bench_reference(args)
     else:

@@ -428,13 +428,14 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         else if (s == "isolver") *out = C.isolver;
         else if (s == "it") *out = (double)C.it;
         else if (s == "cg_iters" || s == "qs_solves" || s == "cg_updates" || s == "cg_carried" ||
-                 s == "guess_tried" || s == "guess_kept") {
+                 s == "guess_tried" || s == "guess_kept" || s == "cg_restarts") {
             Ctrl c;
             EQC_CUDA(cudaMemcpyAsync(&c, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h.stream));
             EQC_CUDA(cudaStreamSynchronize(h.stream));
             *out = (double)(s == "cg_iters" ? c.cg_iters : s == "qs_solves" ? c.cg_solves
                             : s == "cg_updates" ? c.cg_updates : s == "cg_carried" ? c.cg_carried
-                            : s == "guess_tried" ? c.guess_tried : c.guess_kept);
+                            : s == "guess_tried" ? c.guess_tried : s == "guess_kept" ? c.guess_kept
+                            : c.cg_restarts);
         }
         else throw Error(EQC_E_ARG, "unknown scalar " + s);
     });

@@ -30,6 +30,7 @@ struct Ctrl {
     long long cg_solves;   // solves
     long long cg_updates;  // reliable updates (mixed precision)
     long long cg_carried;  // solves that started from the carried residual
+    long long cg_restarts; // reliable updates after which the search direction restarted
     long long guess_tried, guess_kept;   // initial-guess increments judged / kept
     int cg_fail;           // bit 0: a solve reached maxit; bit 1: non-finite residual
     int cg_last_it;        // iterations of the last solve
@@ -47,6 +48,7 @@ struct CGState {
     int it, maxit;
     int done;          // 0 running, 1 converged, 2 maxit reached, 3 non-finite residual
     int need_update;   // mixed precision: a reliable update is due
+    int restart;       // the next direction update starts afresh (beta = 0)
     double sigma;      // mixed precision: the FP32 recurrence vectors hold sigma * (true value),
                        // sigma a power of two near 1 / ||b|| (keeps tiny residuals out of
                        // FP32 underflow); 1 in FP64.  rr is in those scaled units.

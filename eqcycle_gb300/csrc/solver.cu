@@ -51,11 +51,11 @@ __global__ void __launch_bounds__(VEC_THREADS) k_dot_rho(const T* __restrict__ x
     });
 }
 
-// u = z + (rho / rho_prev) u
+// u = z + (rho / rho_prev) u   (u = z after a restart)
 template <class T>
 __global__ void __launch_bounds__(VEC_THREADS) k_pupdate(const T* __restrict__ z, T* __restrict__ u, int64_t n,
-                                                         const double* S) {
-    const T b = (T)(S[S_RHO] / S[S_RHOP]);
+                                                         const double* S, const int* restart) {
+    const T b = *restart ? T(0) : (T)(S[S_RHO] / S[S_RHOP]);
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         T zz[4], uu[4];
         ld4(z + i, zz);
@@ -165,6 +165,7 @@ __global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, cudaGraph
     S->rho = 1.0;
     S->rho_prev = 1.0;
     S->need_update = 0;
+    S->restart = 0;
     const int st = !isfinite(r) ? 3 : (r <= reltol ? 1 : (maxit <= 0 ? 2 : 0));
     S->done = st;
     if (use_cond) cudaGraphSetConditional(hw, st == 0 ? 1u : 0u);
@@ -184,6 +185,7 @@ __global__ void k_cg_check(CGState* S, cudaGraphConditionalHandle hw, int use_co
 // (the recurrence residual fell by `delta` since the last one, or the loop would stop).
 __global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandle hi, int use_cond) {
     S->it += 1;
+    S->restart = 0;   // consumed by this iteration's direction update
     const double rs = sqrt(S->rr) / S->sigma;
     int need = 0;
     if (!isfinite(rs)) {
@@ -203,6 +205,12 @@ __global__ void k_cg_check_b(CGState* S, Ctrl* C, cudaGraphConditionalHandle hw,
     if (S->done != 3) {
         if (S->need_update) {
             const double rs = sqrt(S->rr) / S->sigma;
+            // the true residual left the recurrence's (the FP32 recurrences drifted, e.g. from a
+            // guess far from the solution): continue from the true residual with a fresh direction
+            if (rs > 2.0 * S->res) {
+                S->restart = 1;
+                C->cg_restarts += 1;
+            }
             S->res = rs;
             S->rmax = rs;
             S->need_update = 0;
@@ -386,7 +394,7 @@ static void iter_fp64(Handle& h, cudaGraphConditionalHandle hw, int use_cond) {
     double* q = h.q64.p + ld;
     precond<double>(h, r, z, n);
     k_dot_rho<double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, r, n, h.red_part.p, h.red_count.p, &S->rho);
-    k_pupdate<double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho);
+    k_pupdate<double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho, &S->restart);
     apply_K<double>(h.p64.p, h.q64.p, args64(h), 1.0, 1, h.stream);
     dot64(h, u, q, n, &S->pq);
     k_xr_update<double, double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(x, r, u, q, n, h.red_part.p, h.red_count.p,
@@ -408,7 +416,7 @@ static void iter_mixed_a(Handle& h, double delta, cudaGraphConditionalHandle hi,
     float* y = h.x32.p + ld;   // correction accumulated since the last reliable update
     precond<float>(h, r, z, n);
     k_dot_rho<float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, r, n, h.red_part.p, h.red_count.p, &S->rho);
-    k_pupdate<float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho);
+    k_pupdate<float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho, &S->restart);
     apply_K<float>(h.p32.p, h.q32.p, args32(h), 1.0f, 1, h.stream);
     dot32(h, u, q, n, &S->pq);
     k_xr_update<float, float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(y, r, u, q, n, h.red_part.p, h.red_count.p,

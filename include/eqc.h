@@ -219,7 +219,8 @@ eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
 /* Scalars "t", "dt", "isolver", "it" (and, read-only, the solver counters "cg_iters",
  * "qs_solves", "cg_updates" (reliable updates), "cg_carried" (solves that started from
  * the residual the previous solve left), "guess_tried" / "guess_kept" (initial-guess
- * increments judged against the previous-step guess / kept because they lowered ||r||)).
+ * increments judged against the previous-step guess / kept because they lowered ||r||),
+ * "cg_restarts" (mixed precision: reliable updates after which the CG direction restarted)).
  * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);

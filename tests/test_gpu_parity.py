@@ -281,3 +281,23 @@ def test_ensemble_equals_members_run_alone(eqclib):
     finally:
         for s in solvers:
             s.close()
+
+
+def test_mixed_precision_after_a_dynamic_phase(eqclib):
+    """The first quasi-static solves after dynamic steps start from a displacement far from the
+    quasi-static solution: the mixed solver restarts its direction when the FP64 residual leaves
+    the FP32 recurrence's, converges, and tracks the FP64 method."""
+    cfg = SMALL.replace(V_init=2e-2)
+    P = set_parameters(cfg)
+    out = {}
+    for prec in (EQC_FP64, EQC_MIXED):
+        with Solver(P, precision=prec, precond=EQC_PC_AMG, cg_tol=1e-10) as s:
+            s.init(cfg.V_init)
+            st = s.run(20)
+            assert st["dyn_steps"] >= 15
+            s.set_scalar("isolver", 1)
+            st = s.run(6)
+            assert st["qs_steps"] >= 1
+            out[prec] = ({k: s.state(k) for k in ("d", "v", "psi")}, s.scalar("cg_restarts"))
+    for k in out[EQC_FP64][0]:
+        assert rel(out[EQC_MIXED][0][k], out[EQC_FP64][0][k]) <= 1e-6, k

@@ -132,3 +132,30 @@ def test_guessnet_rounds_every_weight_block_and_no_bias():
     for k, v in W.items():
         want = gn.bf16(np.float32(0.05)) if (k.startswith("cw") or k in ("f1w", "f2w")) else np.float32(0.05)
         assert np.all(v == np.float64(want)), k
+
+
+def test_event_statistics_restatement():
+    """post/earthquake_cycles.jl (Coslip, moment_magnitude_new) restated on a hand-built run."""
+    from eqcycle_gb300.events import catalogue, compare
+    from eqcycle_gb300.solver import Results
+    Nf = 11
+    FltX = np.linspace(-10.0, 0.0, Nf)            # dx = 1
+    slip = np.zeros((Nf, 2))
+    slip[2:5, 0] = [1.0, 2.0, 1.0]
+    slip[5:8, 1] = [0.5, 0.5, 0.001]              # the last node is below 1 % of the maximum
+    tb = np.full((Nf, 2), 30.0)
+    ta = np.full((Nf, 2), 28.0)
+    e = np.zeros(0)
+    res = Results(seismic_stress=e, seismic_slipvel=e, seismic_slip=e, index_eq=e, is_stress=e, is_slipvel=e,
+                  is_slip=e, dSeis=e, vSeis=e, aSeis=e, tStart=np.array([0.0, 100.0]), tEnd=np.array([5.0, 106.0]),
+                  taubefore=tb, tauafter=ta, delfafter=slip, hypo=np.array([-7.0, -4.0]), time_=e, Vfmax=e)
+    mu = 3e10
+    cat = catalogue(res, FltX, mu)
+    assert np.allclose(cat.max_slip, [2.0, 0.5])
+    assert np.allclose(cat.mean_slip, [4.0 / 3.0, 1.0 / 2.0])     # area / zdim over the rupture
+    assert np.allclose(cat.mean_drop, [2.0, 2.0])
+    want_mw0 = (2.0 / 3.0) * np.log10(mu * 4.0 * 3.0 * 1e7) - 10.7
+    assert abs(cat.Mw[0] - want_mw0) < 1e-12
+    assert np.allclose(cat.recurrence, [100.0])
+    c = compare(cat, cat)
+    assert c["compared"] == 2 and c["recurrence"] == 0 and c["coseismic_slip"] == 0 and c["hypocentre_depth"] == 0
