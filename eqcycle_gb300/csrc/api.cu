@@ -219,6 +219,12 @@ static void create(Handle& h, const eqc_model& m) {
     EQC_CUDA(cudaMallocHost(&h.h_scal, sizeof(double) * 16));
     h.cg.alloc(1);
     EQC_CUDA(cudaMallocHost(&h.h_cg, sizeof(CGState)));
+    {   // device logs of batched steps (512 steps, a receiver record every 10th)
+        const int nb = std::max(h.opt.step_batch, 512);
+        h.log_t.alloc(nb);
+        h.log_vf.alloc(nb);
+        h.log_seis.alloc((size_t)(nb / 10 + 2) * 3 * std::max(h.nSeis, 1));
+    }
     std::memset(h.h_cg, 0, sizeof(CGState));
     EQC_CUDA(cudaStreamSynchronize(s));
     if (h.opt.precond == EQC_PC_AMG) mg_build(h);

@@ -19,14 +19,14 @@ void capture_counting(bool on) {
 }
 int64_t capture_tally() { return g_tally; }
 
-cudaGraphConditionalHandle cond_handle(Handle& h) {
+cudaGraphConditionalHandle cond_handle(Handle& h, unsigned dflt) {
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
     EQC_CUDA(cudaStreamGetCaptureInfo(h.stream, &st, nullptr, &g, nullptr, nullptr, nullptr));
     if (st != cudaStreamCaptureStatusActive) throw Error(EQC_E_STATE, "conditional handle outside a capture");
     cudaGraphConditionalHandle c;
-    // reset to 0 at every launch; a kernel upstream of the node sets the value
-    EQC_CUDA(cudaGraphConditionalHandleCreate(&c, g, 0, cudaGraphCondAssignDefault));
+    // reset to dflt at every launch; a kernel upstream of (or inside) the node sets the value
+    EQC_CUDA(cudaGraphConditionalHandleCreate(&c, g, dflt, cudaGraphCondAssignDefault));
     return c;
 }
 

@@ -39,6 +39,11 @@ struct Ctrl {
                            // (mixed precision: carried into the next solve)
     double dt_prev;        // dt of the step before the current one
     int qs_prev;           // the last step was quasi-static: dPre holds the solution before it
+    // batched steps (several steps per graph launch): the host's output-trigger state, written
+    // before each launch, and the device logs' fill counts (k_step_end)
+    double tvsx, tevneb, tevne, t_end, Vthres, Vevne;
+    int slipstart, idelevne, verbose, max_batch, rec_cap;
+    int nlog, nrec;        // steps logged (time_, Vfmax) / receiver records in this launch
 };
 
 // Device-resident scalars of one CG solve.
@@ -82,6 +87,8 @@ struct Handle {
     cudaStream_t cap_streams[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaStream_t> stream_stack;
     StepGraph graphs[2];       // [0] quasi-static step, [1] dynamic step
+    StepGraph batched[2];      // the same, looping over steps on the device (k_step_end)
+    DBuf<double> log_t, log_vf, log_seis;   // per-step device logs of a batched launch
     StepGraph* capturing = nullptr;   // graph whose capture is in progress
     int device = 0;
     Layout L{};
@@ -173,7 +180,7 @@ int qs_solve_device(Handle& h, double tol, int maxit, double* relres);
 // graph.cu
 // Handle of a conditional node of the graph h.stream is capturing (value 0 at each launch
 // unless a kernel upstream of the node sets it).
-cudaGraphConditionalHandle cond_handle(Handle& h);
+cudaGraphConditionalHandle cond_handle(Handle& h, unsigned dflt = 0);
 // Conditional node with handle c on the stream h.stream is capturing; until cond_end,
 // h.stream is the capture stream of the node's body.
 void cond_begin(Handle& h, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle c);
@@ -193,7 +200,8 @@ void enqueue_step(Handle& h, int iso, bool graph);
 struct PostBufs {
     std::vector<double> dF, vF, tauF, seis;
 };
-void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb);
+// logged: the step's time_, Vfmax and receiver records were already taken from the device logs.
+void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb, bool logged = false);
 void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st);
 void fault_slrFunc(Handle& h, const double* psi, double* psi1, const double* Vf, double* Vf1, const double* tau1,
                    double dt);

@@ -467,6 +467,7 @@ void init_state(Handle& h, double V_init) {
 
 // capacities of the reference's preallocated outputs (main.jl:154-163)
 constexpr int64_t CAP_SEISMIC = 30000, CAP_IS = 4000, CAP_SEIS = 190000, CAP_EV = 400, CAP_TIME = 1900000;
+constexpr int STEP_BATCH = 512;   // default steps per batched launch (the size of the device logs)
 
 static void fault_columns(Handle& h, std::vector<double>& dF, std::vector<double>& vF, std::vector<double>& tauF) {
     const int Nf = h.F.Nf;
@@ -557,11 +558,90 @@ void enqueue_step(Handle& h, int iso, bool graph) {
 }
 
 void destroy_graphs(Handle& h) {
-    for (StepGraph& g : h.graphs) {
-        if (g.exec) cudaGraphExecDestroy(g.exec);
-        if (g.graph) cudaGraphDestroy(g.graph);
-        g = StepGraph();
+    for (StepGraph* arr : {h.graphs, h.batched})
+        for (int k = 0; k < 2; ++k) {
+            StepGraph& g = arr[k];
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            if (g.graph) cudaGraphDestroy(g.graph);
+            g = StepGraph();
+        }
+}
+
+// End of a step inside a batched launch: log time_ and Vfmax (and, every 10th step, the receivers,
+// main.jl:433-435), then decide on the device whether the loop of steps goes on.  It stops on any
+// step whose outputs need the host (main.jl:361-436: event start or end, a 5-year snapshot, a
+// seismic snapshot or its end), on a regime switch, a failure flag, t_end, a full log, or verbose
+// progress printing; the host then treats that last step exactly like a single step.
+__global__ void k_step_end(Ctrl* C, double* __restrict__ log_t, double* __restrict__ log_vf,
+                           double* __restrict__ log_seis, const int64_t* __restrict__ iSeis, int ns,
+                           const double* __restrict__ d, const double* __restrict__ v, const double* __restrict__ a,
+                           int regime, cudaGraphConditionalHandle hw) {
+    __shared__ int rec;
+    const long long it = C->it;
+    const int k = C->nlog;
+    if (threadIdx.x == 0) {
+        log_t[k] = C->t;
+        log_vf[k] = C->Vfmax;
+        rec = (ns > 0 && it % 10 == 0) ? C->nrec : -1;
     }
+    __syncthreads();
+    if (rec >= 0 && (int)threadIdx.x < ns) {
+        const int64_t g = iSeis[threadIdx.x];
+        double* o = log_seis + (int64_t)rec * 3 * ns;
+        o[threadIdx.x] = d[g];
+        o[ns + threadIdx.x] = v[g];
+        o[2 * ns + threadIdx.x] = a[g];
+    }
+    if (threadIdx.x == 0) {
+        C->nlog = k + 1;
+        if (rec >= 0) C->nrec = rec + 1;
+        const double t = C->t, Vf = C->Vfmax;
+        int stop = 0;
+        if (C->isolver != regime) stop = 1;
+        if (C->fail != 0x7fffffff || C->apply_err || C->cg_fail || !isfinite(Vf)) stop = 1;
+        if (Vf > 1.01 * C->Vthres && C->slipstart == 0) stop = 1;
+        if (Vf < 0.99 * C->Vthres && C->slipstart == 1) stop = 1;
+        if (t > C->tvsx) stop = 1;
+        if (Vf > C->Vevne) {
+            if (C->idelevne == 0 || (t - C->tevneb) > C->tevne) stop = 1;
+        } else if (C->idelevne == 1) {
+            stop = 1;
+        }
+        if (C->verbose && it % 500 == 0) stop = 1;
+        if (k + 1 >= C->max_batch || t >= C->t_end) stop = 1;
+        if (rec >= 0 && rec + 1 >= C->rec_cap) stop = 1;
+        cudaGraphSetConditional(hw, stop ? 0u : 1u);
+    }
+}
+
+// Captures the batched steps of regime iso: a device-driven WHILE loop over whole steps.
+static StepGraph& batched_graph(Handle& h, int iso) {
+    StepGraph& G = h.batched[iso == 1 ? 0 : 1];
+    if (G.exec) return G;
+    G = StepGraph();
+    h.capturing = &G;
+    capture_counting(true);
+    try {
+        EQC_CUDA(cudaStreamBeginCapture(h.stream, cudaStreamCaptureModeThreadLocal));
+        const cudaGraphConditionalHandle hw = cond_handle(h, 1);   // the first step always runs
+        cond_begin(h, cudaGraphCondTypeWhile, hw);
+        enqueue_step(h, iso, true);
+        k_step_end<<<1, 32, 0, h.stream>>>(h.ctrl.p, h.log_t.p, h.log_vf.p, h.log_seis.p, h.iSeis.p, h.nSeis, h.d.p,
+                                            h.v.p, h.a.p, iso, hw);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+        cond_end(h);
+        EQC_CUDA(cudaStreamEndCapture(h.stream, &G.graph));
+    } catch (...) {
+        abort_capture(h);
+        h.capturing = nullptr;
+        throw;
+    }
+    G.k_fixed = capture_tally() - G.k_bodies;   // kernels of one step (the loop body)
+    capture_counting(false);
+    h.capturing = nullptr;
+    EQC_CUDA(cudaGraphInstantiate(&G.exec, G.graph, 0));
+    return G;
 }
 
 // Captures the step of regime iso (1 quasi-static, 2 dynamic) into a graph, once.
@@ -589,7 +669,7 @@ static StepGraph& step_graph(Handle& h, int iso) {
 
 // Host side of one finished step (the control block is in h.h_ctrl): failure checks and the
 // output triggers of main.jl:361-436.
-void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb) {
+void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb, bool logged) {
     cudaStream_t s = h.stream;
     const int Nf = h.F.Nf;
     const double Vpl = h.Vpl;
@@ -601,10 +681,12 @@ void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb) {
     std::vector<double>& tauF = pb.tauF;
     std::vector<double>& seis = pb.seis;
     if (seis.size() < (size_t)(3 * std::max(h.nSeis, 1))) seis.resize(3 * std::max(h.nSeis, 1));
-    if (iso == 1) stats.qs_steps++;
-    else stats.dyn_steps++;
+    if (!logged) {
+        if (iso == 1) stats.qs_steps++;
+        else stats.dyn_steps++;
+    }
     const double tnow = C.t;
-    h.res.time_.push_back(tnow);
+    if (!logged) h.res.time_.push_back(tnow);
     if (C.fail != 0x7fffffff)
         throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(C.fail));
     if (C.apply_err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
@@ -676,7 +758,7 @@ void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb) {
         h.idelevne = 0;
     }
     if (h.opt.verbose && C.it % 500 == 0) printf("Time (yr) = %1.5g\n", tnow / h.yr2sec);
-    if (C.it % 10 == 0 && h.nSeis > 0) {
+    if (!logged && C.it % 10 == 0 && h.nSeis > 0) {
         if (h.rit >= CAP_SEIS) throw Error(EQC_E_CAPACITY, "receiver capacity (190000) exceeded");
         h.rit += 1;
         k_gather_seis<<<1, 32, 0, s>>>(h.iSeis.p, h.nSeis, h.d.p, h.v.p, h.a.p, h.seis.p);
@@ -689,8 +771,10 @@ void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb) {
             h.res.aSeis.push_back(seis[2 * h.nSeis + k]);
         }
     }
-    h.res.Vfmax.push_back(Vfmax);
-    stats.steps++;
+    if (!logged) {
+        h.res.Vfmax.push_back(Vfmax);
+        stats.steps++;
+    }
 }
 
 void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
@@ -711,9 +795,58 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
     EQC_CUDA(cudaEventCreate(&ev0));
     EQC_CUDA(cudaEventCreate(&ev1));
     EQC_CUDA(cudaEventRecord(ev0, s));
+    const int batch = h.opt.step_batch == 0 ? STEP_BATCH : h.opt.step_batch;
     while (C.t < t_end && stats.steps < max_steps) {
         if ((int64_t)h.res.time_.size() >= CAP_TIME) throw Error(EQC_E_CAPACITY, "time_ capacity (1900000) exceeded");
         const int iso = C.isolver;
+        if (h.opt.use_graphs && batch > 1) {   // several steps per launch, outputs logged on the device
+            const long long it_before = C.cg_iters, up_before = C.cg_updates, ca_before = C.cg_carried,
+                            so_before = C.cg_solves;
+            C.tvsx = h.tvsx;
+            C.tevneb = h.tevneb;
+            C.tevne = h.tevne;
+            C.t_end = t_end;
+            C.Vthres = h.Vthres;
+            C.Vevne = h.Vevne;
+            C.slipstart = (int)h.slipstart;
+            C.idelevne = (int)h.idelevne;
+            C.verbose = h.opt.verbose;
+            C.max_batch = (int)std::min<int64_t>({(int64_t)batch, max_steps - stats.steps,
+                                                  CAP_TIME - (int64_t)h.res.time_.size()});
+            C.rec_cap = (int)std::min<int64_t>(STEP_BATCH / 10 + 2, CAP_SEIS - h.rit);
+            if (h.nSeis > 0 && C.rec_cap < 1) throw Error(EQC_E_CAPACITY, "receiver capacity (190000) exceeded");
+            C.nlog = 0;
+            C.nrec = 0;
+            StepGraph& G = batched_graph(h, iso);
+            EQC_CUDA(cudaMemcpyAsync(h.ctrl.p, h.h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, s));
+            EQC_CUDA(cudaGraphLaunch(G.exec, s));
+            EQC_CUDA(cudaMemcpyAsync(h.h_ctrl, h.ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+            EQC_CUDA(cudaStreamSynchronize(s));
+            const int nl = C.nlog, nr = C.nrec;
+            std::vector<double> lt(nl), lv(nl), ls((size_t)nr * 3 * std::max(h.nSeis, 1));
+            h.log_t.download(lt.data(), nl, s);
+            h.log_vf.download(lv.data(), nl, s);
+            if (nr) h.log_seis.download(ls.data(), (size_t)nr * 3 * h.nSeis, s);
+            EQC_CUDA(cudaStreamSynchronize(s));
+            h.res.time_.insert(h.res.time_.end(), lt.begin(), lt.end());
+            h.res.Vfmax.insert(h.res.Vfmax.end(), lv.begin(), lv.end());
+            for (int r = 0; r < nr; ++r)
+                for (int k = 0; k < h.nSeis; ++k) {
+                    h.res.dSeis.push_back(ls[(size_t)r * 3 * h.nSeis + k]);
+                    h.res.vSeis.push_back(ls[(size_t)r * 3 * h.nSeis + h.nSeis + k]);
+                    h.res.aSeis.push_back(ls[(size_t)r * 3 * h.nSeis + 2 * h.nSeis + k]);
+                }
+            h.rit += nr;
+            stats.steps += nl;
+            if (iso == 1) stats.qs_steps += nl;
+            else stats.dyn_steps += nl;
+            const long long carried = C.cg_carried - ca_before;
+            g_launches += (int64_t)nl * G.k_fixed + G.k_iter * (C.cg_iters - it_before) +
+                          G.k_update * (C.cg_updates - up_before) + G.k_carry * carried +
+                          G.k_full * (C.cg_solves - so_before - carried);
+            post_step(h, iso, stats, pb, true);   // the outputs of the last step (the one that stopped)
+            continue;
+        }
         const long long it_before = C.cg_iters, up_before = C.cg_updates, ca_before = C.cg_carried,
                         so_before = C.cg_solves;
         if (h.opt.use_graphs) {

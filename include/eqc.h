@@ -97,6 +97,10 @@ typedef struct {
                                FP64: persistent TMA pipeline), 1 one tile per CTA by
                                TMA, 2 plain tile loads, 3 persistent TMA pipeline     */
     int32_t mg_degree_coarse; /* Chebyshev steps on the vertex levels (default 3)          */
+    int32_t step_batch;     /* with use_graphs: at most this many time steps per graph launch,
+                               outputs logged on the device (default 0 = 512; 1 = one step per
+                               launch).  A launch ends early at any step whose outputs need
+                               the host (event start/end, snapshots) or on a regime switch. */
 } eqc_options;
 
 typedef struct eqc_handle eqc_handle;

@@ -301,3 +301,27 @@ def test_mixed_precision_after_a_dynamic_phase(eqclib):
             out[prec] = ({k: s.state(k) for k in ("d", "v", "psi")}, s.scalar("cg_restarts"))
     for k in out[EQC_FP64][0]:
         assert rel(out[EQC_MIXED][0][k], out[EQC_FP64][0][k]) <= 1e-6, k
+
+
+def test_batched_steps_equal_single_steps(eqclib):
+    """Steps looped on the device (outputs logged there, the launch ending at any step whose outputs
+    need the host) give the same state and the same results records as one step per launch."""
+    cfg = SMALL.replace(V_init=2e-2)   # fast slip: seismic snapshots, receivers, regime switches
+    P = set_parameters(cfg)
+    out = []
+    for batch in (1, 0):
+        with Solver(P, precision=EQC_FP64, precond=EQC_PC_AMG, step_batch=batch) as s:
+            s.init(cfg.V_init)
+            st = s.run(150)
+            out.append((st, {k: s.state(k) for k in ("d", "v", "psi")}, s.results()))
+    (st1, x1, r1), (st0, x0, r0) = out
+    assert st0["dyn_steps"] > 20
+    for k in ("steps", "qs_steps", "dyn_steps", "cg_iters"):
+        assert st0[k] == st1[k], k
+    for k in x1:
+        assert np.array_equal(x0[k], x1[k]), k
+    for f in ("time_", "Vfmax", "dSeis", "vSeis", "aSeis", "seismic_slip", "seismic_stress", "tStart", "hypo",
+              "taubefore", "is_slip"):
+        a, b = getattr(r0, f), getattr(r1, f)
+        assert a.shape == b.shape and np.array_equal(a, b), f
+    assert len(r1.dSeis) > 0 and r1.seismic_slip.shape[1] > 0
