@@ -125,7 +125,7 @@ static void create(Handle& h, const eqc_model& m) {
     std::vector<double> Mlay(N, 1.0);
     for (int64_t g = 0; g < m.nglob; ++g) Mlay[h.ref2lay[g]] = m.M[g];
     for (DBuf<double>* b : {&h.M, &h.d, &h.v, &h.a, &h.dPre, &h.tmp64a, &h.tmp64b, &h.tmp64c, &h.r64, &h.z64, &h.p64,
-                             &h.q64})
+                             &h.q64, &h.Kd})
         b->alloc(N);
     for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32, &h.g32}) b->alloc(N);
     h.M.upload(Mlay.data(), N, s);

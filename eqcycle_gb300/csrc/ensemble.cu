@@ -62,7 +62,7 @@ static void ensemble_capture(eqc_ensemble& E) {
                 cond_begin(h, cudaGraphCondTypeIf, reg == 1 ? hq : hd);
                 enqueue_step(h, reg, true);
                 cond_end(h);
-                G.k_fixed = (capture_tally() - t0) - G.k_bodies + 1;   // + the selector
+                G.k_fixed = (capture_tally() - t0) - G.k_bodies + G.k_fixed_extra + 1;   // + the selector
                 h.capturing = nullptr;
             }
             EQC_CUDA(cudaEventRecord(E.ev[1 + m], h.stream));

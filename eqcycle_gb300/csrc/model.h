@@ -44,7 +44,11 @@ struct Ctrl {
     double tvsx, tevneb, tevne, t_end, Vthres, Vevne;
     int slipstart, idelevne, verbose, max_batch, rec_cap;
     int nlog, nrec;        // steps logged (time_, Vfmax) / receiver records in this launch
+    // mixed-precision Newmark: Kd = K d kept in FP64, updated by the FP32 apply of each step's
+    // increment and refreshed in FP64 at the start of a dynamic phase and every KD_REFRESH steps
+    int kd_valid, kd_age, kd_full;
 };
+constexpr int KD_REFRESH = 256;
 
 // Device-resident scalars of one CG solve.
 struct CGState {
@@ -71,6 +75,7 @@ struct StepGraph {
     int64_t k_carry = 0;     // kernels of a carried residual set-up (if body)
     int64_t k_full = 0;      // kernels of a full residual set-up (if body)
     int64_t k_bodies = 0;    // capture tally of all conditional bodies
+    int64_t k_fixed_extra = 0;   // kernels of if-bodies that run every step (one of a pair)
 };
 
 // Multigrid hierarchy (defined in mg.h), learned-guess network (learn.h).
@@ -105,6 +110,7 @@ struct Handle {
     double H[25];
     // node arrays [L.size()]
     DBuf<double> M, d, v, a, dPre, tmp64a, tmp64b, tmp64c;
+    DBuf<double> Kd;          // K d of the mixed-precision dynamic step
     DBuf<double> diag64;   // diagonal of K (rows >= 1), Jacobi preconditioner
     DBuf<float> diag32;
     // boundary lists (layout indices) and coefficients

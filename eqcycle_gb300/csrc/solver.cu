@@ -545,7 +545,8 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry, con
 void invalidate_residual(Handle& h) {
     EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->r_valid, 0, sizeof(int), h.stream));
     EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->qs_prev, 0, sizeof(int), h.stream));
-    if (h.h_ctrl) h.h_ctrl->r_valid = h.h_ctrl->qs_prev = 0;
+    EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->kd_valid, 0, sizeof(int), h.stream));
+    if (h.h_ctrl) h.h_ctrl->r_valid = h.h_ctrl->qs_prev = h.h_ctrl->kd_valid = 0;
 }
 
 // Solves for d_I given d row 0 = F (eager); returns iterations (negative: maxit reached).

@@ -104,8 +104,9 @@ __global__ void __launch_bounds__(FNT) k_qs_end_fault(double* __restrict__ v, Fa
 
 // v[FltNI] = (d - dPre)/dt ; a = 0  (main.jl:289-292), rows >= 1
 __global__ void k_qs_end_bulk(const double* __restrict__ d, const double* __restrict__ dPre, double* __restrict__ v,
-                              double* __restrict__ a, int64_t ld, int64_t n, const Ctrl* C) {
+                              double* __restrict__ a, int64_t ld, int64_t n, Ctrl* C) {
     const double dt = C->dt;
+    if (blockIdx.x == 0 && threadIdx.x == 0) C->kd_valid = 0;   // d changed: no incremental K d
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         if (i >= ld) v[i] = (d[i] - dPre[i]) / dt;
         a[i] = 0.;
@@ -136,6 +137,53 @@ __global__ void k_dyn_predict(double* __restrict__ d, double* __restrict__ v, co
         if (i < Nf) vPre_f[i] = vi;
         d[i] = d[i] + dt * vi + (hdt2)*ai;
         v[i] = vi + hdt * ai;
+    }
+}
+
+// Mixed-precision predictor: the increment dd = dt v + dt^2/2 a in FP64, d += dd, dd32 = (float) dd.
+__global__ void k_dyn_predict_inc(double* __restrict__ d, double* __restrict__ v, const double* __restrict__ a,
+                                  double* __restrict__ vPre_f, float* __restrict__ dd32, int Nf, int64_t n, Ctrl* C) {
+    const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        C->r_valid = 0;
+        C->qs_prev = 0;
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double vi = v[i], ai = a[i];
+        if (i < Nf) vPre_f[i] = vi;
+        const double dd = dt * vi + hdt2 * ai;
+        d[i] = d[i] + dd;
+        dd32[i] = (float)dd;
+        v[i] = vi + hdt * ai;
+    }
+}
+
+// Chooses how this step gets K d: a full FP64 apply (start of a dynamic phase, every KD_REFRESH
+// steps) or the FP32 apply of the increment.
+__global__ void k_kd_select(Ctrl* C, cudaGraphConditionalHandle hf, cudaGraphConditionalHandle hi, int use_cond) {
+    const int full = (!C->kd_valid || C->kd_age >= KD_REFRESH) ? 1 : 0;
+    C->kd_full = full;
+    if (use_cond) {
+        cudaGraphSetConditional(hf, full ? 1u : 0u);
+        cudaGraphSetConditional(hi, full ? 0u : 1u);
+    }
+}
+
+// a = -K d with K d either refreshed (Kd written by the FP64 apply) or Kd += K dd (t32, FP32).
+__global__ void k_dyn_force(double* __restrict__ Kd, const float* __restrict__ t32, double* __restrict__ a, int64_t n,
+                            Ctrl* C) {
+    const int full = C->kd_full;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double k = Kd[i];
+        if (!full) {
+            k += (double)t32[i];
+            Kd[i] = k;
+        }
+        a[i] = -k;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        C->kd_valid = 1;
+        C->kd_age = full ? 0 : C->kd_age + 1;
     }
 }
 
@@ -527,13 +575,46 @@ static void enqueue_qs(Handle& h, bool graph) {
 }
 
 // Dynamic step (main.jl:297-345): Newmark predictor, K d, boundaries, fault, corrector.
-static void enqueue_dyn(Handle& h) {
+static void enqueue_dyn(Handle& h, bool graph) {
     cudaStream_t s = h.stream;
     const int64_t n = h.L.size();
     FaultArgs f = fargs(h, h.bcflag.p);
-    k_dyn_predict<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.F.Nf, n, h.ctrl.p);
-    count_launch();
-    apply_K<double>(h.d.p, h.a.p, args64(h), -1.0, 0, s);
+    if (h.opt.precision == EQC_MIXED) {
+        // FP64 accumulation of d and of K d, FP32 apply of the step's increment
+        k_dyn_predict_inc<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n, h.ctrl.p);
+        count_launch();
+        if (graph) {
+            const cudaGraphConditionalHandle hf = cond_handle(h), hi = cond_handle(h);
+            k_kd_select<<<1, 1, 0, s>>>(h.ctrl.p, hf, hi, 1);
+            count_launch();
+            const int64_t t0 = capture_tally();
+            cond_begin(h, cudaGraphCondTypeIf, hf);
+            apply_K<double>(h.d.p, h.Kd.p, args64(h), 1.0, 0, h.stream);
+            cond_end(h);
+            const int64_t t1 = capture_tally();
+            cond_begin(h, cudaGraphCondTypeIf, hi);
+            apply_K<float>(h.g32.p, h.q32.p, args32(h), 1.0f, 0, h.stream);
+            cond_end(h);
+            if (h.capturing) {
+                h.capturing->k_bodies += capture_tally() - t0;
+                h.capturing->k_fixed_extra += std::max(t1 - t0, capture_tally() - t1);   // one of the two runs
+            }
+        } else {
+            k_kd_select<<<1, 1, 0, s>>>(h.ctrl.p, 0, 0, 0);
+            count_launch();
+            int full = 0;
+            EQC_CUDA(cudaMemcpyAsync(&full, &h.ctrl.p->kd_full, sizeof(int), cudaMemcpyDeviceToHost, s));
+            EQC_CUDA(cudaStreamSynchronize(s));
+            if (full) apply_K<double>(h.d.p, h.Kd.p, args64(h), 1.0, 0, s);
+            else apply_K<float>(h.g32.p, h.q32.p, args32(h), 1.0f, 0, s);
+        }
+        k_dyn_force<<<vblocks(n), 256, 0, s>>>(h.Kd.p, h.q32.p, h.a.p, n, h.ctrl.p);
+        count_launch();
+    } else {
+        k_dyn_predict<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.F.Nf, n, h.ctrl.p);
+        count_launch();
+        apply_K<double>(h.d.p, h.a.p, args64(h), -1.0, 0, s);
+    }
     k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p, h.BcTC.p,
                                 h.nBcT);
     k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
@@ -551,7 +632,7 @@ void enqueue_step(Handle& h, int iso, bool graph) {
     k_step_begin<<<1, 1, 0, h.stream>>>(h.ctrl.p);
     count_launch();
     if (iso == 1) enqueue_qs(h, graph);
-    else enqueue_dyn(h);
+    else enqueue_dyn(h, graph);
     k_control<<<1, FT, 0, h.stream>>>(h.v.p, fargs(h, h.bcflag.p), h.ctrl.p);
     launch_check();
     count_launch();
@@ -637,7 +718,7 @@ static StepGraph& batched_graph(Handle& h, int iso) {
         h.capturing = nullptr;
         throw;
     }
-    G.k_fixed = capture_tally() - G.k_bodies;   // kernels of one step (the loop body)
+    G.k_fixed = capture_tally() - G.k_bodies + G.k_fixed_extra;   // kernels of one step (the loop body)
     capture_counting(false);
     h.capturing = nullptr;
     EQC_CUDA(cudaGraphInstantiate(&G.exec, G.graph, 0));
@@ -660,7 +741,7 @@ static StepGraph& step_graph(Handle& h, int iso) {
         h.capturing = nullptr;
         throw;
     }
-    G.k_fixed = capture_tally() - G.k_bodies;
+    G.k_fixed = capture_tally() - G.k_bodies + G.k_fixed_extra;
     capture_counting(false);
     h.capturing = nullptr;
     EQC_CUDA(cudaGraphInstantiate(&G.exec, G.graph, 0));

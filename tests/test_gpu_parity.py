@@ -325,3 +325,14 @@ def test_batched_steps_equal_single_steps(eqclib):
         a, b = getattr(r0, f), getattr(r1, f)
         assert a.shape == b.shape and np.array_equal(a, b), f
     assert len(r1.dSeis) > 0 and r1.seismic_slip.shape[1] > 0
+
+
+def test_mixed_dynamic_steps_match_oracle(eqclib, oracle_mod):
+    """The mixed method's Newmark steps (FP64 d and K d, FP32 apply of each step's increment, FP64
+    refresh of K d at the start of the phase) against the FP64 oracle."""
+    cfg = SMALL.replace(V_init=2e-2)
+    P, o, st, got, ref, res = _run_both(cfg, 60, oracle_mod, 1e-12, precision=EQC_MIXED, precond=EQC_PC_AMG)
+    assert st["dyn_steps"] >= 30
+    for k in ("d", "v", "psi", "tau"):
+        assert rel(got[k], ref[k]) <= 1e-6, k
+    assert rel(res.Vfmax, o.get("Vfmax")) <= 1e-6
