@@ -129,6 +129,13 @@ static void create(Handle& h, const eqc_model& m) {
         b->alloc(N);
     for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32, &h.g32}) b->alloc(N);
     h.M.upload(Mlay.data(), N, s);
+    {
+        std::vector<double> inv(N);
+        for (int64_t i = 0; i < N; ++i) inv[i] = 1.0 / Mlay[i];
+        h.invM.alloc(N);
+        h.invM.upload(inv.data(), N, s);
+        EQC_CUDA(cudaStreamSynchronize(s));
+    }
     std::vector<double> dg = diag_K(h, m.W);
     for (int64_t i = 0; i < N; ++i)   // fault row and row padding are not part of the system
         if (i < L.ld || (i % L.ld) >= L.nx) dg[i] = 1.0;

@@ -111,6 +111,7 @@ struct Handle {
     // node arrays [L.size()]
     DBuf<double> M, d, v, a, dPre, tmp64a, tmp64b, tmp64c;
     DBuf<double> Kd;          // K d of the mixed-precision dynamic step
+    DBuf<double> invM;        // 1 / M (mixed-precision dynamic step)
     DBuf<double> diag64;   // diagonal of K (rows >= 1), Jacobi preconditioner
     DBuf<float> diag32;
     // boundary lists (layout indices) and coefficients

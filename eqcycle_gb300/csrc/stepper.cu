@@ -19,7 +19,7 @@
 namespace eqc {
 
 constexpr int FT = 1024;  // threads of the single-CTA fault-row reductions
-constexpr int FNT = 128;  // threads per CTA of the per-node fault kernels
+constexpr int FNT = 32;   // threads per CTA of the per-node fault kernels (FP64 Newton: spread over SMs)
 static inline int fblocks(int Nf) { return (Nf + FNT - 1) / FNT; }
 
 // ---------------------------------------------------------------- quasi-static kernels
@@ -229,12 +229,13 @@ __global__ void __launch_bounds__(FNT) k_dyn_fault(double* __restrict__ a, const
     }
 }
 
-// a = a / M ; v += dt/2 a   (main.jl:336-339)
+// a = a / M ; v += dt/2 a   (main.jl:336-339).  inv: M holds 1/M (mixed method: a multiply
+// instead of GB300's slow FP64 division; the plain method divides as the reference does).
 __global__ void k_dyn_correct(double* __restrict__ a, double* __restrict__ v, const double* __restrict__ M, int64_t n,
-                              const Ctrl* C) {
+                              const Ctrl* C, int inv) {
     const double hdt = C->half_dt;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double ai = a[i] / M[i];
+        const double ai = inv ? a[i] * M[i] : a[i] / M[i];
         a[i] = ai;
         v[i] = v[i] + hdt * ai;
     }
@@ -247,36 +248,30 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
     __shared__ double smax[FT / 32];
     __shared__ int sidx[FT / 32];
     __shared__ double smin[FT / 32];
+    __shared__ int s_next;
     const double Vpl = C->Vpl;
     const double dtmax = 50.0 * 24 * 60 * 60;
-    double vmax = -INFINITY, dmin = dtmax;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // Vfmax and its first index, the regime of the next step
+    double vmax = -INFINITY;
     int imax = 0x7fffffff;
     for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) {
         const double vk = v[k];
         if (vk > vmax) { vmax = vk; imax = k; }
-        if (k >= f.NFBC0) {
-            const double sr = fabs(2 * vk + Vpl);
-            if (sr * dtmax > f.XiLf[k]) dmin = fmin(dmin, f.XiLf[k] / sr);
-        }
     }
-    // warp reductions: max with first index, min
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const double ov = __shfl_down_sync(0xffffffffu, vmax, o);
         const int oi = __shfl_down_sync(0xffffffffu, imax, o);
         if (ov > vmax || (ov == vmax && oi < imax)) { vmax = ov; imax = oi; }
-        dmin = fmin(dmin, __shfl_down_sync(0xffffffffu, dmin, o));
     }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) { smax[w] = vmax; sidx[w] = imax; smin[w] = dmin; }
+    if (lane == 0) { smax[w] = vmax; sidx[w] = imax; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double bv = -INFINITY, bm = dtmax;
+        double bv = -INFINITY;
         int bi = 0x7fffffff;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q)
             if (smax[q] > bv || (smax[q] == bv && sidx[q] < bi)) { bv = smax[q]; bi = sidx[q]; }
-            bm = fmin(bm, smin[q]);
-        }
         const double Vfmax = 2 * bv + Vpl;
         C->Vfmax = Vfmax;
         C->vhypo = Vfmax;
@@ -284,18 +279,32 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
         const int iso = C->isolver;
         const int next = ((iso == 1 && Vfmax < 5e-3) || (iso == 2 && Vfmax < 2e-3)) ? 1 : 2;
         C->isolver = next;
-        double dt;
-        if (next == 1) {
-            double dtnx = bm;
-            if (C->dtmin > dtnx) dtnx = C->dtmin;
-            if (dtnx > 1.2 * C->dt) dtnx = 1.2 * C->dt;
-            dt = dtnx;
-        } else {
-            dt = C->dtmin;
-        }
         C->dt_prev = C->dt;
         if (iso == 1) C->qs_prev = 1;
-        C->dt = dt;
+        s_next = next;
+        if (next == 2) C->dt = C->dtmin;   // dtevol!: the dynamic step takes dtmin
+    }
+    __syncthreads();
+    if (s_next != 1) return;
+    // dtevol! for a quasi-static next step: min over XiLf / |V|, capped at 1.2 dt
+    double dmin = dtmax;
+    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) {
+        if (k >= f.NFBC0) {
+            const double sr = fabs(2 * v[k] + Vpl);
+            if (sr * dtmax > f.XiLf[k]) dmin = fmin(dmin, f.XiLf[k] / sr);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_down_sync(0xffffffffu, dmin, o));
+    if (lane == 0) smin[w] = dmin;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bm = dtmax;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) bm = fmin(bm, smin[q]);
+        double dtnx = bm;
+        if (C->dtmin > dtnx) dtnx = C->dtmin;
+        if (dtnx > 1.2 * C->dt_prev) dtnx = 1.2 * C->dt_prev;
+        C->dt = dtnx;
     }
 }
 
@@ -618,7 +627,8 @@ static void enqueue_dyn(Handle& h, bool graph) {
     k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p, h.BcTC.p,
                                 h.nBcT);
     k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
-    k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, h.M.p, n, h.ctrl.p);
+    const bool mixed = h.opt.precision == EQC_MIXED;
+    k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, mixed ? h.invM.p : h.M.p, n, h.ctrl.p, mixed ? 1 : 0);
     count_launch(3);
     if (h.nCreep) {
         k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, h.a.p, nullptr);
