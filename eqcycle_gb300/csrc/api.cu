@@ -437,6 +437,8 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         const std::string s(name);
         const Ctrl& C = *h.h_ctrl;
         if (s == "t") *out = C.t;
+        else if (s == "apply_variant") *out = h.opt.apply_variant;
+        else if (s == "reliable_delta") *out = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : 1e-3;
         else if (s == "dt") *out = C.dt;
         else if (s == "isolver") *out = C.isolver;
         else if (s == "it") *out = (double)C.it;

@@ -1,7 +1,11 @@
-// Solver autotuner: picks the Chebyshev smoothing degrees of the multigrid V-cycle (spectral-
-// element level and vertex levels) by timing graph-replayed trial solves of the next
-// quasi-static solve of the current model.  Which pair is fastest depends on the mesh (a
-// cheaper coarse smoother can cost more CG iterations), so it is measured, not fixed.
+// Solver autotuner: picks, by timing graph-replayed trial solves of the next quasi-static solve
+// of the current model, (1) the Chebyshev smoothing degrees of the multigrid V-cycle (spectral-
+// element level and vertex levels), then, in mixed precision, (2) the FP32 stiffness-apply
+// kernel and its tile shape (element rows per CTA, or the TMA-fed walk with its one-wave grid)
+// and (3) the residual-replacement factor of the reliable updates.  Which choice is fastest
+// depends on the mesh (a cheaper coarse smoother can cost more CG iterations; a tile shape
+// changes the number of waves; fewer FP64 updates can cost restarts), so it is measured, not
+// fixed.
 #include "model.h"
 #include "mg.h"
 #include <cstring>
@@ -92,6 +96,29 @@ extern "C" eqc_status eqc_autotune(eqc_handle* H, int32_t reps, int32_t* deg_out
         m.deg_coarse = best_c;
         h.opt.mg_degree = best_d;
         h.opt.mg_degree_coarse = best_c;
+        if (h.opt.precision == EQC_MIXED) {
+            // FP32 apply: 6 element rows per CTA (3 or 2 CTAs per SM), 4 rows, or the walk
+            const int v0 = h.opt.apply_variant;
+            int best_v = v0;
+            for (int v : {0, 7, 4, 8}) {
+                if (v == v0) continue;
+                h.opt.apply_variant = v;
+                int it = 0;
+                const double ms = trial(h, d0.p, reps, &it);
+                if (ms < best) { best = ms; best_v = v; }
+            }
+            h.opt.apply_variant = best_v;
+            // reliable-update factor
+            const double r0 = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : 1e-3;
+            double best_r = r0;
+            for (double r : {1e-2, 1e-4}) {
+                h.opt.reliable_delta = r;
+                int it = 0;
+                const double ms = trial(h, d0.p, reps, &it);
+                if (ms < best) { best = ms; best_r = r; }
+            }
+            h.opt.reliable_delta = best_r;
+        }
         // the state and the counters as they were; the trial solves overwrote the residual
         EQC_CUDA(cudaMemcpyAsync(h.d.p, dsave.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         EQC_CUDA(cudaMemcpyAsync(h.ctrl.p, csave.p, sizeof(Ctrl), cudaMemcpyDeviceToDevice, s));

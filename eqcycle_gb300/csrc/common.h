@@ -91,9 +91,9 @@ struct Layout {
 // TMA tensor maps of the stiffness apply: one per node vector (keyed by its address) and
 // one for the padded element data, per precision.
 struct TmaCache {
-    bool ok = false;
-    std::unordered_map<const void*, CUtensorMap> u32, u64;
-    CUtensorMap w32, w64;
+    bool ok = false, walk_ok = false;
+    std::unordered_map<const void*, CUtensorMap> u32, u64, u32walk;
+    CUtensorMap w32, w64, w32walk;
 };
 
 // W padded to a 16-byte multiple per element, so element tiles are TMA-addressable.

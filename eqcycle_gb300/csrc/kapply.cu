@@ -605,6 +605,149 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const floa
     }
 }
 
+// ---- element-per-lane apply fed by TMA, walking up the strips (FP32) ------------------------
+// The grid is one wave (every CTA resident at once).  CTA b walks strip b % nsx (31 element
+// columns plus the halo lane) upward through element rows [r0, r0 + rw), rw = 8 L - 1, in L
+// tiles of 8 element rows, one per warp.  Each tile's node rows (one 132 x 33 box) and element
+// records (one 28 x 32 x 8 box of the padded W copy) arrive by TMA into one of two stages while
+// the other stage's tile is computed, so a CTA never waits on memory between its tiles.  In the
+// first tile warp 0 computes the row below the walk (top row only: the halo); in later tiles the
+// row below warp 0 is the previous tile's warp 7, whose top-row contributions are carried in
+// shared memory.  Coordinates outside the mesh read as zero (virtual elements have W = 0).  The
+// arithmetic and the order of the carries are those of k_apply_rows: both give the same bits.
+constexpr int WK_ROWS = 8, WK_UX = 132, WK_UY = 4 * WK_ROWS + 1;
+constexpr int WK_U_BYTES = WK_UX * WK_UY * 4;                     // 17,424
+constexpr int WK_W_BYTES = 28 * 32 * WK_ROWS * 4;                 // 28,672
+constexpr int WK_W_OFF = ((WK_U_BYTES + 127) / 128) * 128;
+constexpr int WK_STAGE = WK_W_OFF + WK_W_BYTES;
+constexpr int WK_TS_OFF = 2 * WK_STAGE;                           // [2][ROWS][5][32] floats
+constexpr int WK_BAR_OFF = WK_TS_OFF + 2 * WK_ROWS * 5 * 32 * 4;
+constexpr int WK_BYTES = WK_BAR_OFF + 16;
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+// orders this thread's earlier generic-proxy shared-memory accesses before later TMA writes
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_constant__ CUtensorMap umap,
+                                                                const __grid_constant__ CUtensorMap wmap,
+                                                                float* __restrict__ y, ApplyArgs<float> A, float sign,
+                                                                int zero_row0, int nsx, int rw) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const Layout L = A.L;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int ex0 = 31 * ((int)blockIdx.x % nsx);   // element of lane 1
+    const int r0 = ((int)blockIdx.x / nsx) * rw;
+    const int r_end = min(r0 + rw, L.NelY + 1);     // element row NelY is the virtual top row
+    const int nt = (r_end - r0 + WK_ROWS) / WK_ROWS;  // tiles cover rows r0 - 1 .. r_end - 1
+    float* Ts = reinterpret_cast<float*>(smem + WK_TS_OFF);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + WK_BAR_OFF);
+    auto issue = [&](int k) {
+        const int st = k & 1, base = r0 - 1 + WK_ROWS * k;
+        mbar_expect_tx(&bar[st], (uint32_t)(WK_U_BYTES + WK_W_BYTES));
+        tma_load_2d(smem + st * WK_STAGE, &umap, &bar[st], 4 * (ex0 - 1), 4 * base);
+        tma_load_3d(smem + st * WK_STAGE + WK_W_OFF, &wmap, &bar[st], 0, ex0 - 1, base);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        issue(0);
+        if (nt > 1) issue(1);
+    }
+    const int ex = ex0 - 1 + lane;
+    for (int k = 0; k < nt; ++k) {
+        const int st = k & 1;
+        const uint32_t parity = (uint32_t)((k >> 1) & 1);
+        bool done = false;
+        for (int it = 0; it < MBAR_SPIN_LIMIT && !done; ++it) done = mbar_try_wait(&bar[st], parity);
+        if (__syncthreads_or(!done)) {
+            // give up: flag it, wait (bounded) for the copies still in flight (tiles k, k + 1), leave
+            if (threadIdx.x == 0) {
+                if (A.err) atomicExch(A.err, 1);
+                for (int j = k; j < nt && j < k + 2; ++j)
+                    for (int it = 0; it < MBAR_SPIN_LIMIT; ++it)
+                        if (mbar_try_wait(&bar[j & 1], (uint32_t)((j >> 1) & 1))) break;
+            }
+            return;
+        }
+        const int ey = r0 - 1 + WK_ROWS * k + w;
+        const float* xs = reinterpret_cast<const float*>(smem + st * WK_STAGE) + 4 * w * WK_UX;
+        const float* wsm = reinterpret_cast<const float*>(smem + st * WK_STAGE + WK_W_OFF) + (w * 32 + lane) * 28;
+        float u[5][5];
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            const float4 v = *reinterpret_cast<const float4*>(xs + j * WK_UX + 4 * lane);
+            u[j][0] = v.x;
+            u[j][1] = v.y;
+            u[j][2] = v.z;
+            u[j][3] = v.w;
+            const float n4 = __shfl_down_sync(FULLMASK, v.x, 1);
+            u[j][4] = lane == 31 ? xs[j * WK_UX + 128] : n4;
+        }
+        float W[28];
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+            const float4 c = *reinterpret_cast<const float4*>(wsm + 4 * q);
+            W[4 * q] = c.x;
+            W[4 * q + 1] = c.y;
+            W[4 * q + 2] = c.z;
+            W[4 * q + 3] = c.w;
+        }
+        const bool halo = k == 0 && w == 0;
+        float out[4][4], R[4], T[5];
+        rows_lines(u, W, A.c1, A.c2, halo, out, R, T);
+        float* Tk = Ts + st * (WK_ROWS * 160);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) Tk[(w * 5 + i) * 32 + lane] = T[i];
+        float Rl[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) Rl[j] = __shfl_up_sync(FULLMASK, R[j], 1);
+        // warp 0 after the first tile: the top row of the previous tile's warp 7 (written before
+        // the previous tile's barrier, overwritten only after this tile's)
+        float cb[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        if (w == 0 && k > 0) {
+            const float* Tp = Ts + (st ^ 1) * (WK_ROWS * 160) + (WK_ROWS - 1) * 160;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cb[i] = Tp[i * 32 + lane];
+            cb[4] = Tp[4 * 32 + (lane > 0 ? lane - 1 : 0)];
+        }
+        __syncthreads();   // T of every warp written; every read of this stage done
+        if (threadIdx.x == 0 && k + 2 < nt) {
+            fence_proxy_async_smem();
+            issue(k + 2);
+        }
+        if (lane == 0 || halo || ex > L.NelX || ey > L.NelY || ey >= r_end) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) out[j][0] += Rl[j];
+        if (w > 0) {
+            const float* Tb = Tk + (w - 1) * 160;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) out[0][i] += Tb[i * 32 + lane];
+            out[0][0] += Tb[4 * 32 + lane - 1];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) out[0][i] += cb[i];
+            out[0][0] += cb[4];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int iy = 4 * ey + j;
+            if (iy >= L.ny) break;
+            const float z = (zero_row0 && iy == 0) ? 0.f : sign;
+            *reinterpret_cast<float4*>(y + (int64_t)iy * L.ld + 4 * ex) =
+                make_float4(z * out[j][0], z * out[j][1], z * out[j][2], z * out[j][3]);
+        }
+    }
+}
+
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                      const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                      CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -632,6 +775,19 @@ static bool encode_2d(CUtensorMap* m, bool f64, const void* base, uint64_t d0, u
     return fn(m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base),
               dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// W of the walk apply as a 3-D tensor [NelY][NelX][28] with a 28 x 32 x WK_ROWS box.
+static bool encode_w_walk(CUtensorMap* m, const float* base, int NelX, int NelY) {
+    PFN_encodeTiled fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {28, (cuuint64_t)NelX, (cuuint64_t)NelY};
+    const cuuint64_t strides[2] = {28 * sizeof(float), (cuuint64_t)NelX * 28 * sizeof(float)};
+    const cuuint32_t box[3] = {28, 32, WK_ROWS};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 constexpr int TEX = 8, TEY = 8;
@@ -669,10 +825,23 @@ static const CUtensorMap* tma_umap(TmaCache& c, const T* x, const Layout& L) {
     return &(m[x] = tm);
 }
 
+// Node-vector map of the walk apply (cached by address): box WK_UX x WK_UY.
+static const CUtensorMap* tma_umap_walk(TmaCache& c, const float* x, const Layout& L) {
+    if (!c.walk_ok) return nullptr;
+    auto it = c.u32walk.find(x);
+    if (it != c.u32walk.end()) return &it->second;
+    if ((reinterpret_cast<uintptr_t>(x) & 15) != 0) return nullptr;
+    CUtensorMap tm;
+    if (!encode_2d(&tm, false, x, (uint64_t)L.nx, (uint64_t)L.ny, (uint64_t)L.ld * sizeof(float), WK_UX, WK_UY))
+        return nullptr;
+    return &(c.u32walk[x] = tm);
+}
+
 // Encodes the element-data maps; leaves the cache disabled (plain loads) if TMA is unavailable.
 void tma_init(Handle& h) {
     TmaCache& c = h.tma;
     c.ok = false;
+    c.walk_ok = false;
     if (getenv("EQC_NO_TMA")) return;
     const Layout& L = h.L;
     const int EX = LTEX + 1, EY = LTEY + 1;
@@ -681,6 +850,7 @@ void tma_init(Handle& h) {
     ok = ok && encode_2d(&c.w64, true, h.W64p.p, (uint64_t)L.NelX * WPad<double>::v, (uint64_t)L.NelY,
                          (uint64_t)L.NelX * WPad<double>::v * sizeof(double), EX * WPad<double>::v, EY);
     c.ok = ok;
+    c.walk_ok = ok && encode_w_walk(&c.w32walk, h.W32p.p, L.NelX, L.NelY);
 }
 
 // CTAs of the pipelined apply: as many as fit on every SM at once.
@@ -699,6 +869,39 @@ static void pipe_setup() {
     g_pipe_blocks[sizeof(T) == 8 ? 1 : 0] = std::max(1, per_sm) * nsm;
 }
 
+// CTAs of the walk apply that are resident at once (its grid never exceeds one wave).
+static int g_walk_slots = 0;
+static void walk_setup() {
+    EQC_CUDA(cudaFuncSetAttribute(k_apply_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, WK_BYTES));
+    int per_sm = 0, dev = 0, nsm = 0;
+    EQC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_walk, 32 * WK_ROWS, WK_BYTES));
+    EQC_CUDA(cudaGetDevice(&dev));
+    EQC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    g_walk_slots = std::max(1, per_sm) * nsm;
+}
+
+// Walk length: the fewest tiles per walk whose walks all fit in one wave.
+static void walk_shape(const Layout& L, int* nsx, int* rw, int* nblk) {
+    *nsx = (L.NelX + 1 + 30) / 31;
+    const int rows = L.NelY + 1;
+    int tiles = 1;
+    while (tiles < rows && (int64_t)*nsx * ((rows + 8 * tiles - 2) / (8 * tiles - 1)) > g_walk_slots) ++tiles;
+    *rw = WK_ROWS * tiles - 1;
+    *nblk = *nsx * ((rows + *rw - 1) / *rw);
+}
+
+static bool launch_walk(const float* x, float* y, const ApplyArgs<float>& A, float sign, int zr, cudaStream_t s) {
+    if (!A.tma || !A.tma->walk_ok || g_walk_slots <= 0) return false;
+    const CUtensorMap* um = tma_umap_walk(*A.tma, x, A.L);
+    if (!um) return false;
+    int nsx, rw, nblk;
+    walk_shape(A.L, &nsx, &rw, &nblk);
+    k_apply_walk<<<nblk, 32 * WK_ROWS, WK_BYTES, s>>>(*um, A.tma->w32walk, y, A, sign, zr, nsx, rw);
+    EQC_CHECK_LAUNCH();
+    count_launch();
+    return true;
+}
+
 void set_H(const double* H, cudaStream_t s) {
     float hf[25];
     for (int k = 0; k < 25; ++k) hf[k] = (float)H[k];
@@ -712,6 +915,7 @@ void set_H(const double* H, cudaStream_t s) {
                                   (int)apply_smem<float>()));
     pipe_setup<float>();
     pipe_setup<double>();
+    walk_setup();
 
 }
 
@@ -741,6 +945,8 @@ void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStre
     if (mode <= 1) {
         dim3 grid(A.L.NelX / LTEX + 1, A.L.NelY / LTEY + 1);
         if constexpr (sizeof(T) == 4) {
+            if (A.variant == 8 && A.Wp && aligned16(x) && aligned16(y) && launch_walk(x, y, A, sign, mode == 1 ? 1 : 0, s))
+                return;
             if ((A.variant == 0 || A.variant >= 4) && A.Wp && aligned16(x) && aligned16(y)) {
                 launch_rows(x, y, A, sign, mode == 1 ? 1 : 0, s);
                 return;

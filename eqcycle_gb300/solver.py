@@ -178,10 +178,13 @@ class Solver:
         self._chk(L.lib().eqc_set_state(self.h, name.encode(), L.dptr(_c(value, np.float64))))
 
     def autotune(self, reps: int = 2):
-        """Choose the multigrid smoothing degrees by timed trial solves (state unchanged)."""
+        """Choose the multigrid smoothing degrees and, in mixed precision, the FP32 apply kernel
+        and the reliable-update factor by timed trial solves (state unchanged)."""
         dg, dc, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
         self._chk(L.lib().eqc_autotune(self.h, reps, C.byref(dg), C.byref(dc), C.byref(ms)))
-        return {"mg_degree": dg.value, "mg_degree_coarse": dc.value, "solve_ms": ms.value}
+        return {"mg_degree": dg.value, "mg_degree_coarse": dc.value, "solve_ms": ms.value,
+                "apply_variant": int(self.scalar("apply_variant")),
+                "reliable_delta": self.scalar("reliable_delta")}
 
     # -- learned initial guess
     def guess_shape(self):

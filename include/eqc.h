@@ -94,8 +94,12 @@ typedef struct {
     int32_t mg_cluster_max; /* > 0: levels with at most this many grid points run as one
                                thread-block-cluster launch (default 0: off)            */
     int32_t apply_variant;  /* stiffness apply kernel: 0 default (FP32: one element per lane,
-                               FP64: persistent TMA pipeline), 1 one tile per CTA by
-                               TMA, 2 plain tile loads, 3 persistent TMA pipeline     */
+                               6 element rows per CTA; FP64: persistent TMA pipeline),
+                               1 one tile per CTA by TMA, 2 plain tile loads, 3 persistent
+                               TMA pipeline, FP32 only: 4 / 5 / 6 / 7 one element per lane
+                               with 4 / 8 / 12 / 6 (2 CTAs per SM) element rows per CTA,
+                               8 one element per lane fed by TMA, one wave of CTAs each
+                               walking up a strip of 31 element columns                 */
     int32_t mg_degree_coarse; /* Chebyshev steps on the vertex levels (default 3)          */
     int32_t step_batch;     /* with use_graphs: at most this many time steps per graph launch,
                                outputs logged on the device (default 0 = 512; 1 = one step per
@@ -224,7 +228,8 @@ eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
  * "qs_solves", "cg_updates" (reliable updates), "cg_carried" (solves that started from
  * the residual the previous solve left), "guess_tried" / "guess_kept" (initial-guess
  * increments judged against the previous-step guess / kept because they lowered ||r||),
- * "cg_restarts" (mixed precision: reliable updates after which the CG direction restarted)).
+ * "cg_restarts" (mixed precision: reliable updates after which the CG direction restarted),
+ * and the solver settings "apply_variant" and "reliable_delta" (as chosen by eqc_autotune)).
  * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);
@@ -267,9 +272,12 @@ eqc_status eqc_time_apply(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t fl
 
 /* Solver autotuner (no counterpart in the reference): times `reps` graph-replayed trial
  * solves of the next quasi-static solve from the current state for a set of Chebyshev
- * degrees (spectral-element level x vertex levels) and keeps the fastest; the state and the
- * counters are restored.  *mg_degree, *mg_degree_coarse and *solve_ms (all optional) get the
- * choice and its trial time.  Call after eqc_init (or between eqc_run calls). */
+ * degrees (spectral-element level x vertex levels) and keeps the fastest; in mixed precision
+ * it then tries the FP32 apply kernels (apply_variant 0, 7, 4, 8) and the reliable-update
+ * factors 1e-2, 1e-3, 1e-4 in turn.  The state and the counters are restored.  *mg_degree,
+ * *mg_degree_coarse and *solve_ms (all optional) get the choice and its trial time; the
+ * apply kernel and the factor chosen are the scalars "apply_variant" and "reliable_delta"
+ * (eqc_get_scalar).  Call after eqc_init (or between eqc_run calls). */
 eqc_status eqc_autotune(eqc_handle* h, int32_t reps, int32_t* mg_degree, int32_t* mg_degree_coarse, double* solve_ms);
 
 /* Kernel launches of the library since the handle was created. */

@@ -221,6 +221,7 @@ def test_autotune_keeps_the_state_and_chooses_a_valid_smoother(eqclib):
                 scal = {k: s.scalar(k) for k in ("t", "dt", "isolver", "cg_iters", "qs_solves")}
                 res = s.autotune(reps=1)
                 assert res["mg_degree"] in (3, 4, 5) and res["mg_degree_coarse"] in (1, 3, 4)
+                assert res["apply_variant"] in (0, 7, 4, 8) and res["reliable_delta"] in (1e-2, 1e-3, 1e-4)
                 assert res["solve_ms"] > 0
                 for k, v in before.items():
                     assert np.array_equal(s.state(k), v), k
