@@ -25,6 +25,7 @@ own replica and value sums the ranks' simulated years over the slowest rank's ti
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -63,25 +64,78 @@ def _allreduce(dist, v, op):
     return float(t.item())
 
 
+# FP32 apply kernels by eqc_options.apply_variant
+APPLY_KERNELS = {0: "k_apply_rows<6,3>", 4: "k_apply_rows<4,3>", 5: "k_apply_rows<8,2>", 6: "k_apply_rows<12,1>",
+                 7: "k_apply_rows<6,2>", 8: "k_apply_walk"}
+
+
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """SM clock and clock-event (throttle) reasons sampled every 2 ms during the timed region,
+    read through NVML (libnvidia-ml, read-only queries); nvidia-smi at 200 ms if NVML cannot
+    be loaded."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, device: int):
+        import threading
+        self.samples, self.smax, self.mask = [], 0.0, 0
         self.p = None
+        self.stop_ev = threading.Event()
+        self.th = None
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                raise OSError("nvmlInit")
+            cnt = ctypes.c_uint(0)
+            nv.nvmlDeviceGetCount_v2(ctypes.byref(cnt))
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+            idx = device
+            if cnt.value == 1:
+                idx = 0
+            elif vis and all(x.strip().isdigit() for x in vis.split(",")):
+                idx = int(vis.split(",")[device])
+            h = ctypes.c_void_p()
+            if nv.nvmlDeviceGetHandleByIndex_v2(idx, ctypes.byref(h)) != 0:
+                raise OSError("nvmlDeviceGetHandleByIndex")
+            mx = ctypes.c_uint(0)
+            nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))   # NVML_CLOCK_SM
+            self.smax = float(mx.value)
+
+            def run():
+                clk, rs = ctypes.c_uint(0), ctypes.c_ulonglong(0)
+                while not self.stop_ev.is_set():
+                    if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0:
+                        self.samples.append(float(clk.value))
+                    if nv.nvmlDeviceGetCurrentClocksEventReasons(h, ctypes.byref(rs)) == 0:
+                        self.mask |= int(rs.value)
+                    time.sleep(0.002)
+            self.th = threading.Thread(target=run, daemon=True)
+            self.th.start()
+            return
+        except Exception:
+            self.th = None
         self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
-            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.Q}",
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 
     def stop(self):
+        if self.th is not None:
+            self.stop_ev.set()
+            self.th.join(timeout=5)
+            if not self.samples:
+                return None
+            return {"sm_mhz": float(np.median(self.samples)), "sm_max_mhz": self.smax,
+                    "reasons": sorted(n for b, n in self.REASONS.items() if self.mask & b),
+                    "samples": len(self.samples), "source": "nvml, 2 ms"}
         if self.p is None:
             return None
         self.p.terminate()
@@ -107,7 +161,7 @@ class Clocks:
         if not sm:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 def steady_dt(solver, P):
@@ -237,10 +291,12 @@ def bench_ours(args):
     bytes32 = 4 * (2 * nglob + 25 * Nel)
     ms64 = s.time_apply(0, 20, True)
     bytes64 = 8 * (2 * nglob + 25 * Nel)
+    # DRAM bytes per launch of the kernel the autotuner chose, from one ncu capture
+    kname = APPLY_KERNELS.get(tuned.get("apply_variant", 0), "k_apply_rows<6,3>")
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "kapply_dz480_traffic.json")
+    tp = os.path.join(ROOT, "profiles", f"kapply_{args.workload}_traffic.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("fp32_bytes_per_launch")
+        traffic = json.load(open(tp)).get("fp32_bytes_per_launch", {}).get(kname)
     s.close()
     # ---- the same window with the previous-step guess (the reference's), and with the learned
     # guess trained on pairs the plain solver logs on 8 other seeds of the workload
@@ -296,7 +352,8 @@ def bench_ours(args):
                 "d2h_bytes_per_step": d2h / args.steps},
         "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": bytes32 / (ms32 * 1e-3) / 1e9 / peak, "traffic": traffic,
-                     "kernel": "k_apply_rows<6,3> (FP32 stiffness apply, one element per lane)", "peak_kind": peak_kind,
+                     "kernel": f"{kname} (FP32 stiffness apply, one element per lane; chosen by the autotuner)",
+                     "peak_kind": peak_kind,
                      "launch_us": ms32 * 1e3, "algorithmic_bytes": bytes32},
         "fp64_apply": {"launch_us": ms64 * 1e3, "algorithmic_bytes": bytes64,
                        "achieved_gbs": bytes64 / (ms64 * 1e-3) / 1e9},

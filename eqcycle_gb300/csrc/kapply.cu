@@ -607,8 +607,8 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const floa
 
 // ---- element-per-lane apply fed by TMA, walking up the strips (FP32) ------------------------
 // The grid is one wave (every CTA resident at once).  CTA b walks strip b % nsx (31 element
-// columns plus the halo lane) upward through element rows [r0, r0 + rw), rw = 8 L - 1, in L
-// tiles of 8 element rows, one per warp.  Each tile's node rows (one 132 x 33 box) and element
+// columns plus the halo lane) upward through element rows [r0, r0 + rw) in tiles of 8 element
+// rows, one per warp (warps past the walk's last row sit the last tile out).  Each tile's node rows (one 132 x 33 box) and element
 // records (one 28 x 32 x 8 box of the padded W copy) arrive by TMA into one of two stages while
 // the other stage's tile is computed, so a CTA never waits on memory between its tiles.  In the
 // first tile warp 0 computes the row below the walk (top row only: the halo); in later tiles the
@@ -679,6 +679,14 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
             return;
         }
         const int ey = r0 - 1 + WK_ROWS * k + w;
+        if (ey >= r_end) {   // past the walk (warp-uniform): no row to compute, only the barrier
+            __syncthreads();
+            if (threadIdx.x == 0 && k + 2 < nt) {
+                fence_proxy_async_smem();
+                issue(k + 2);
+            }
+            continue;
+        }
         const float* xs = reinterpret_cast<const float*>(smem + st * WK_STAGE) + 4 * w * WK_UX;
         const float* wsm = reinterpret_cast<const float*>(smem + st * WK_STAGE + WK_W_OFF) + (w * 32 + lane) * 28;
         float u[5][5];
@@ -880,14 +888,15 @@ static void walk_setup() {
     g_walk_slots = std::max(1, per_sm) * nsm;
 }
 
-// Walk length: the fewest tiles per walk whose walks all fit in one wave.
+// Walk length: the rows of every strip split evenly over the resident CTAs (one wave, every
+// SM holding the same number of rows to within one walk).
 static void walk_shape(const Layout& L, int* nsx, int* rw, int* nblk) {
     *nsx = (L.NelX + 1 + 30) / 31;
-    const int rows = L.NelY + 1;
-    int tiles = 1;
-    while (tiles < rows && (int64_t)*nsx * ((rows + 8 * tiles - 2) / (8 * tiles - 1)) > g_walk_slots) ++tiles;
-    *rw = WK_ROWS * tiles - 1;
-    *nblk = *nsx * ((rows + *rw - 1) / *rw);
+    const int64_t rows = L.NelY + 1;
+    int64_t r = std::max<int64_t>(1, (rows * *nsx + g_walk_slots - 1) / g_walk_slots);
+    while (r < rows && *nsx * ((rows + r - 1) / r) > g_walk_slots) ++r;
+    *rw = (int)r;
+    *nblk = *nsx * (int)((rows + r - 1) / r);
 }
 
 static bool launch_walk(const float* x, float* y, const ApplyArgs<float>& A, float sign, int zr, cudaStream_t s) {
