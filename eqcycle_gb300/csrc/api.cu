@@ -45,6 +45,62 @@ static std::vector<double> diag_K(const Handle& h, const double* W) {
     return dg;
 }
 
+// W (FP64, FP32, and both copies padded per element for TMA element tiles) and the diagonal
+// of K on the device.  Buffers are allocated once; a later call (damage evolution) rewrites
+// them in place, so the tensor maps of the element data stay valid.
+static void load_element_data(Handle& h, const double* W) {
+    const Layout& L = h.L;
+    cudaStream_t s = h.stream;
+    const int64_t Nel = (int64_t)L.NelX * L.NelY;
+    const size_t nW = (size_t)25 * Nel;
+    const bool first = h.W64.p == nullptr;
+    if (first) {
+        h.W64.alloc(nW);
+        h.W32.alloc(nW);
+        h.W32p.alloc((size_t)WPad<float>::v * Nel);
+        h.W64p.alloc((size_t)WPad<double>::v * Nel);
+        h.diag64.alloc(L.size());
+        h.diag32.alloc(L.size());
+    }
+    std::vector<float> w32(nW);
+    for (size_t k = 0; k < nW; ++k) w32[k] = (float)W[k];
+    const int p32 = WPad<float>::v, p64 = WPad<double>::v;
+    std::vector<float> a((size_t)p32 * Nel, 0.f);
+    std::vector<double> b((size_t)p64 * Nel, 0.0);
+    for (int64_t e = 0; e < Nel; ++e)
+        for (int q = 0; q < 25; ++q) {
+            a[(size_t)p32 * e + q] = w32[(size_t)25 * e + q];
+            b[(size_t)p64 * e + q] = W[(size_t)25 * e + q];
+        }
+    std::vector<double> dg = diag_K(h, W);
+    for (int64_t i = 0; i < L.size(); ++i)   // fault row and row padding are not part of the system
+        if (i < L.ld || (i % L.ld) >= L.nx) dg[i] = 1.0;
+    std::vector<float> dg32(dg.begin(), dg.end());
+    h.W64.upload(W, nW, s);
+    h.W32.upload(w32.data(), nW, s);
+    h.W32p.upload(a.data(), a.size(), s);
+    h.W64p.upload(b.data(), b.size(), s);
+    h.diag64.upload(dg.data(), dg.size(), s);
+    h.diag32.upload(dg32.data(), dg32.size(), s);
+    EQC_CUDA(cudaStreamSynchronize(s));
+}
+
+void damage_evolve(Handle& h) {
+    if (h.damage_el.empty()) return;
+    const int64_t Nel = (int64_t)h.L.NelX * h.L.NelY;
+    std::vector<double> W((size_t)25 * Nel);
+    h.W64.download(W.data(), W.size(), h.stream);
+    EQC_CUDA(cudaStreamSynchronize(h.stream));
+    for (int64_t e : h.damage_el)   // damageEvol!: W[:, :, damage_idx] .*= factor
+        for (int q = 0; q < 25; ++q) W[(size_t)25 * e + q] *= h.damage_factor;
+    load_element_data(h, W.data());
+    if (h.opt.precond == EQC_PC_AMG) mg_build(h);   // K changed: new Galerkin hierarchy and bounds
+    invalidate_residual(h);   // carried residual, extrapolation history and K d refer to the old K
+    destroy_graphs(h);        // the step graphs hold the old hierarchy's buffers
+    h.damage_count += 1;
+    h.gen += 1;
+}
+
 static void create(Handle& h, const eqc_model& m) {
     fail_if(m.NGLL != 5, "NGLL must be 5");
     fail_if(m.NelX < 1 || m.NelY < 1 || m.Nel != m.NelX * m.NelY, "Nel != NelX*NelY");
@@ -98,27 +154,7 @@ static void create(Handle& h, const eqc_model& m) {
         fail_if(h.ref2lay[m.iFlt[k] - 1] != k, "iFlt must run along the y = 0 edge from x = -LX (BoundaryMatrix 'B')");
 
     // element data
-    const size_t nW = (size_t)25 * m.Nel;
-    h.W64.alloc(nW);
-    h.W64.upload(m.W, nW, s);
-    std::vector<float> w32(nW);
-    for (size_t k = 0; k < nW; ++k) w32[k] = (float)m.W[k];
-    h.W32.alloc(nW);
-    h.W32.upload(w32.data(), nW, s);
-    {   // copies padded per element for TMA element tiles
-        const int p32 = WPad<float>::v, p64 = WPad<double>::v;
-        std::vector<float> a((size_t)p32 * m.Nel, 0.f);
-        std::vector<double> b((size_t)p64 * m.Nel, 0.0);
-        for (int64_t e = 0; e < m.Nel; ++e)
-            for (int q = 0; q < 25; ++q) {
-                a[(size_t)p32 * e + q] = w32[(size_t)25 * e + q];
-                b[(size_t)p64 * e + q] = m.W[(size_t)25 * e + q];
-            }
-        h.W32p.alloc(a.size());
-        h.W32p.upload(a.data(), a.size(), s);
-        h.W64p.alloc(b.size());
-        h.W64p.upload(b.data(), b.size(), s);
-    }
+    load_element_data(h, m.W);
 
     // node arrays
     const int64_t N = L.size();
@@ -136,14 +172,6 @@ static void create(Handle& h, const eqc_model& m) {
         h.invM.upload(inv.data(), N, s);
         EQC_CUDA(cudaStreamSynchronize(s));
     }
-    std::vector<double> dg = diag_K(h, m.W);
-    for (int64_t i = 0; i < N; ++i)   // fault row and row padding are not part of the system
-        if (i < L.ld || (i % L.ld) >= L.nx) dg[i] = 1.0;
-    std::vector<float> dg32(dg.begin(), dg.end());
-    h.diag64.alloc(N);
-    h.diag64.upload(dg.data(), N, s);
-    h.diag32.alloc(N);
-    h.diag32.upload(dg32.data(), N, s);
 
     // boundary lists
     auto to_lay = [&](const int64_t* idx, int64_t n) {
@@ -438,6 +466,7 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         const Ctrl& C = *h.h_ctrl;
         if (s == "t") *out = C.t;
         else if (s == "apply_variant") *out = h.opt.apply_variant;
+        else if (s == "damage_events") *out = (double)h.damage_count;
         else if (s == "reliable_delta") *out = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : 1e-3;
         else if (s == "dt") *out = C.dt;
         else if (s == "isolver") *out = C.isolver;
@@ -531,6 +560,28 @@ eqc_status eqc_layout(eqc_handle* H, int64_t* nx, int64_t* ny, int64_t* ld) {
     if (ny) *ny = H->h.L.ny;
     if (ld) *ld = H->h.L.ld;
     return EQC_OK;
+}
+
+eqc_status eqc_set_damage(eqc_handle* H, const int64_t* damage_idx, int64_t n, double factor) {
+    if (!H || n < 0 || (n > 0 && !damage_idx) || !(factor > 0.0) || !std::isfinite(factor)) return EQC_E_ARG;
+    return guarded(H, [&] {
+        Handle& h = H->h;
+        const int64_t Nel = (int64_t)h.L.NelX * h.L.NelY;
+        std::vector<int64_t> el((size_t)n);
+        for (int64_t k = 0; k < n; ++k) {
+            fail_if(damage_idx[k] < 1 || damage_idx[k] > Nel, "damage_idx entries must be element numbers 1..Nel");
+            el[(size_t)k] = damage_idx[k] - 1;
+        }
+        std::sort(el.begin(), el.end());
+        el.erase(std::unique(el.begin(), el.end()), el.end());
+        h.damage_el = std::move(el);
+        h.damage_factor = factor;
+    });
+}
+
+eqc_status eqc_damage_evolve(eqc_handle* H) {
+    if (!H) return EQC_E_ARG;
+    return guarded(H, [&] { damage_evolve(H->h); });
 }
 
 eqc_status eqc_apply_K_device(eqc_handle* H, const void* x, void* y, int32_t dtype) {

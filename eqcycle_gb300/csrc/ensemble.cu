@@ -29,10 +29,16 @@ struct eqc_ensemble {
     std::vector<cudaEvent_t> ev;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    std::vector<int64_t> gens;       // members' K generations at capture (damage evolution)
     std::string err;
-    ~eqc_ensemble() {
+    void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+    ~eqc_ensemble() {
+        drop_graph();
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -83,6 +89,14 @@ static void ensemble_capture(eqc_ensemble& E) {
     }
     capture_counting(false);
     EQC_CUDA(cudaGraphInstantiate(&E.exec, E.graph, 0));
+    E.gens.resize(n);
+    for (size_t m = 0; m < n; ++m) E.gens[m] = E.mem[m]->gen;
+}
+
+// A member whose K changed (damage evolution) invalidates the captured ensemble step.
+static void check_gens(eqc_ensemble& E) {
+    for (size_t m = 0; m < E.mem.size() && E.exec; ++m)
+        if (m >= E.gens.size() || E.gens[m] != E.mem[m]->gen) E.drop_graph();
 }
 
 }  // namespace eqc
@@ -133,6 +147,7 @@ eqc_status eqc_ensemble_run(eqc_ensemble* E, int64_t steps, eqc_run_stats* stats
     try {
         for (Handle* h : E->mem)
             if (!h->initialized) throw Error(EQC_E_STATE, "ensemble member not initialised (eqc_init)");
+        check_gens(*E);
         if (!E->exec) ensemble_capture(*E);
         cudaStream_t s0 = E->stream;
         auto t0 = std::chrono::steady_clock::now();
@@ -159,6 +174,8 @@ eqc_status eqc_ensemble_run(eqc_ensemble* E, int64_t steps, eqc_run_stats* stats
                 before[m] = *E->mem[m]->h_ctrl;
                 iso[m] = before[m].isolver;
             }
+            check_gens(*E);
+            if (!E->exec) ensemble_capture(*E);
             EQC_CUDA(cudaGraphLaunch(E->exec, s0));
             for (size_t m = 0; m < n; ++m)
                 EQC_CUDA(cudaMemcpyAsync(E->mem[m]->h_ctrl, E->mem[m]->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, s0));

@@ -85,6 +85,12 @@ struct GuessNet;
 struct Handle {
     eqc_options opt{};
     std::string err;
+    // damage evolution (damageEvol.jl): elements (0-based) whose W is scaled by damage_factor
+    // at the end of every event; gen counts changes of K (graphs holding the old K are stale)
+    std::vector<int64_t> damage_el;
+    double damage_factor = 1.0;
+    int64_t damage_count = 0;
+    int64_t gen = 0;
     // Stream that work is enqueued on: the handle's own stream, or, while a conditional
     // body of a step graph is being captured, that body's capture stream.
     cudaStream_t stream = nullptr;
@@ -201,6 +207,7 @@ int64_t capture_tally();
 // stepper.cu
 void init_state(Handle& h, double V_init);
 void destroy_graphs(Handle& h);
+void damage_evolve(Handle& h);
 // One whole time step of regime iso (1 quasi-static, 2 dynamic) on h.stream; graph: inside a capture.
 void enqueue_step(Handle& h, int iso, bool graph);
 // Host side of a finished step (control block already in h.h_ctrl): checks and outputs.

@@ -814,6 +814,8 @@ void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb, bool logg
         push_col(h.res.tauafter, 2);
         h.res.tEnd.push_back(tnow);
         h.slipstart = 0;
+        // damage grows at the end of each earthquake (main.jl:377-378, damageEvol.jl:5-7)
+        if (!h.damage_el.empty() && h.damage_factor != 1.0) damage_evolve(h);
     }
     if (tnow > h.tvsx) {
         if (h.ntvsx >= CAP_IS) throw Error(EQC_E_CAPACITY, "interseismic snapshot capacity (4000) exceeded");

@@ -255,6 +255,11 @@ def set_parameters(cfg: ModelConfig) -> Params:
         rho_e = np.broadcast_to(r_el[None, None, :], (5, 5, Nel))
         mu_e = np.broadcast_to(m_el[None, None, :], (5, 5, Nel))
     muMax = float(mu_e.max())
+    # elements of the damage zone (Assemble.jl:25-35 returns them as damage_idx): the rectangle
+    # rule, or, for the per-node trapezoid, every element holding a damaged node
+    mu1 = cfg.rho1 * (cfg.vs1 * cfg.vs1)
+    damage_idx = (np.nonzero(np.any(mu_e.reshape(25, Nel) != mu1, axis=0))[0] + 1 if cfg.damage
+                  else np.zeros(0, dtype=np.int64)).astype(np.int64)
     W = wg2[:, :, None] * mu_e
     W = np.asfortranarray(W)
     # lumped mass, accumulated element by element (Assemble.jl:165)
@@ -379,4 +384,5 @@ def set_parameters(cfg: ModelConfig) -> Params:
         iarray=ParamsIarray(iFlt + 1, iBcL + 1, iBcT + 1, FltIglobBC + 1, FltNI + 1, out_seis + 1),
         mesh=Mesh(NelX, NelY, NGLL, dxe, dye, iglob, W, H, xgll, wgll, x, y, muMax),
         cfg=cfg,
+        extra={"damage_idx": damage_idx},
     )

@@ -262,6 +262,17 @@ class Solver:
         kw = {f: self.result(f) for f in Results.__dataclass_fields__ if f != "index_eq"}
         return Results(index_eq=np.zeros(0), **kw)
 
+    # -- damage evolution (damageEvol.jl)
+    def set_damage(self, damage_idx=None, factor: float = 0.95):
+        """Scale W of these elements (1-based; default: the model's damage zone) by ``factor`` at
+        the end of every event."""
+        idx = self.P.extra.get("damage_idx", np.zeros(0, np.int64)) if damage_idx is None else damage_idx
+        a = np.ascontiguousarray(idx, dtype=np.int64)
+        self._chk(L.lib().eqc_set_damage(self.h, a.ctypes.data_as(C.POINTER(C.c_int64)), len(a), float(factor)))
+
+    def damage_evolve(self):
+        self._chk(L.lib().eqc_damage_evolve(self.h))
+
     def time_apply(self, dtype: int = 0, nrep: int = 20, flush_l2: bool = True) -> float:
         ms = C.c_double(0)
         self._chk(L.lib().eqc_time_apply(self.h, dtype, nrep, int(flush_l2), C.byref(ms)))

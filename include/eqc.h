@@ -229,7 +229,8 @@ eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
  * the residual the previous solve left), "guess_tried" / "guess_kept" (initial-guess
  * increments judged against the previous-step guess / kept because they lowered ||r||),
  * "cg_restarts" (mixed precision: reliable updates after which the CG direction restarted),
- * and the solver settings "apply_variant" and "reliable_delta" (as chosen by eqc_autotune)).
+ * the solver settings "apply_variant" and "reliable_delta" (as chosen by eqc_autotune), and
+ * "damage_events" (damage steps applied, eqc_set_damage)).
  * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);
@@ -254,6 +255,19 @@ eqc_status eqc_ensemble_create(eqc_handle* const* members, int32_t n, eqc_ensemb
 eqc_status eqc_ensemble_run(eqc_ensemble* e, int64_t steps, eqc_run_stats* stats, double* gpu_ms);
 eqc_status eqc_ensemble_destroy(eqc_ensemble* e);
 const char* eqc_ensemble_last_error(const eqc_ensemble* e);
+
+/* ---- damage evolution (damageEvol.jl:5-7; its call at the end of each event,
+ * main.jl:377-378, is commented out in the reference, so it is off unless set here) */
+
+/* Elements (1-based, the numbering of W: e = (ey-1)*NelX + ex) whose weights W[:, :, e] are
+ * multiplied by `factor` at the end of every event of eqc_run (damageEvol.jl uses 0.95, on
+ * the damage_idx that Assemble.jl:25-35 returns).  K changes with W, so the multigrid
+ * hierarchy is rebuilt and the solver's carried state is dropped.  n = 0 turns it off. */
+eqc_status eqc_set_damage(eqc_handle* h, const int64_t* damage_idx, int64_t n, double factor);
+
+/* Apply one damage step now (the same scaling and rebuild as at an event end).  The scalar
+ * "damage_events" counts the steps applied. */
+eqc_status eqc_damage_evolve(eqc_handle* h);
 
 /* ---- device-resident entry points (benchmarks, integration with device codes) */
 

@@ -45,6 +45,7 @@ ArrRef lookup(const orc_model* m, const std::string& s) {
     if (s == "H") return D(m->H);
     if (s == "W") return D(m->W);
     if (s == "iglob") return I(m->iglob);
+    if (s == "damage_idx") return I(m->damage_idx);
     if (s == "M") return D(m->M);
     if (s == "BcLC") return D(m->BcLC);
     if (s == "BcTC") return D(m->BcTC);
@@ -171,6 +172,7 @@ extern "C" double orc_scalar(const orc_model* m, const char* name) {
     if (s == "amg_levels") {
         return (double)m->amg.levels.size() + (m->qs_ready ? 1 : 0);
     }
+    if (s == "damage_count") return (double)m->damage_count;
     if (s == "amg_complexity") return m->qs_ready ? m->amg.operator_complexity() : -1.0;
     if (s == "amg_coarse") return (double)m->amg.nc;
     if (s == "n_events") return (double)m->out.tStart.size();
@@ -198,3 +200,15 @@ extern "C" int orc_set_state(orc_model* m, const char* name, const void* in) {
     else return -1;
     return 0;
 }
+
+extern "C" int orc_set_damage(orc_model* m, const int64_t* idx, int64_t n, double factor) {
+    m->damage_el.clear();
+    for (int64_t k = 0; k < n; ++k) {
+        if (idx[k] < 1 || idx[k] > m->Nel) return -1;
+        m->damage_el.push_back(idx[k] - 1);
+    }
+    m->damage_factor = factor;
+    return 0;
+}
+
+extern "C" void orc_damage_evolve(orc_model* m) { orc::damage_evolve(m); }

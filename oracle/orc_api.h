@@ -113,6 +113,11 @@ void orc_reset(orc_model* m);
 int orc_state(const orc_model* m, const char* name, void* out);
 int orc_set_state(orc_model* m, const char* name, const void* in);
 
+/* Damage evolution (damageEvol.jl): elements (1-based) whose W is scaled by factor at every
+ * event end of orc_run, or now by orc_damage_evolve; K is assembled again. */
+int  orc_set_damage(orc_model* m, const int64_t* idx, int64_t n, double factor);
+void orc_damage_evolve(orc_model* m);
+
 void orc_set_threads(int n);
 int  orc_get_threads(void);
 

@@ -69,6 +69,10 @@ struct orc_model {
     orc::vec W;               // [NGLL,NGLL,Nel]
     orc::vec rho_node, mu_node;   // trapezoid per-node properties (damage 2)
     orc::CSR K;               // assembled stiffness, reference numbering
+    orc::ivec damage_idx;     // 0-based elements of the damage zone (Assemble.jl:25-35)
+    orc::ivec damage_el;      // elements whose W is scaled at every event end (damageEvol.jl)
+    double damage_factor = 1.0;
+    int64_t damage_count = 0;
     // params_farray (par.jl:268-292)
     orc::vec fo, Vo, xLf, M, BcLC, BcTC, FltB, FltZ, FltX, cca, ccb, Seff, tauo, XiLf, xout, yout;
     // params_iarray (par.jl:294-301), 0-based
@@ -96,6 +100,8 @@ struct orc_model {
 
 namespace orc {
 void setup_model(orc_model* m);
+void assemble_K(orc_model* m);
+void damage_evolve(orc_model* m);
 void gll(int ngll, double* x, double* w, double* H);
 void init_state(orc_model* m);
 void qs_prepare(orc_model* m);

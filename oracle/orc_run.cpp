@@ -186,6 +186,8 @@ extern "C" int64_t orc_run(orc_model* m, int64_t nsteps, double t_end_s, int qs_
             record_fault(m, m->out.tauafter, 2);
             m->out.tEnd.push_back(tnow);
             m->slipstart = 0;
+            // damage grows at the end of each earthquake (main.jl:377-378)
+            if (!m->damage_el.empty() && m->damage_factor != 1.0) orc::damage_evolve(m);
         }
         // interseismic snapshots (main.jl:384-393)
         if (tnow > m->tvsx) {

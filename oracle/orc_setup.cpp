@@ -133,6 +133,53 @@ static void csr_from_coo(int64_t n, std::vector<int64_t>& I, std::vector<int64_t
     }
 }
 
+// Stiffness assembly from the element weights W (Kassemble.jl:3-63): the element matrix of
+// every element, summed into CSR through the connectivity (FEMSparse's COO sum).
+void assemble_K(orc_model* m) {
+    const int NGLL = 5;
+    const int64_t nglob = (int64_t)m->x.size();
+    auto IG = [&](int i, int j, int64_t e) { return m->iglob[i + NGLL * j + (int64_t)NGLL * NGLL * e]; };
+    const double* H = m->H.data();
+    auto Hm = [&](int i, int j) { return H[i + NGLL * j]; };
+    const double cy = m->jac / (m->dy_deta * m->dy_deta);  // multiplies the eta terms
+    const double cx = m->jac / (m->dx_dxi * m->dx_dxi);
+    std::vector<int64_t> I, J;
+    vec V;
+    const size_t per = (size_t)NGLL * NGLL * (2 * NGLL - 1);
+    I.reserve(per * m->Nel);
+    J.reserve(per * m->Nel);
+    V.reserve(per * m->Nel);
+    for (int64_t eo = 0; eo < m->Nel; ++eo) {
+        const double* ww = &m->W[(int64_t)NGLL * NGLL * eo];
+        auto w = [&](int i, int j) { return ww[i + NGLL * j]; };
+        for (int l = 0; l < NGLL; ++l)
+            for (int k = 0; k < NGLL; ++k)
+                for (int j = 0; j < NGLL; ++j)
+                    for (int i = 0; i < NGLL; ++i) {
+                        if (i != k && j != l) continue;
+                        double term1 = 0.0, term2 = 0.0;
+                        for (int p = 0; p < NGLL; ++p) {
+                            term1 += (i == k ? 1.0 : 0.0) * w(k, p) * cy * Hm(j, p) * Hm(l, p);
+                            term2 += (j == l ? 1.0 : 0.0) * w(p, j) * cx * Hm(i, p) * Hm(k, p);
+                        }
+                        I.push_back(IG(i, j, eo));
+                        J.push_back(IG(k, l, eo));
+                        V.push_back(term1 + term2);
+                    }
+    }
+    csr_from_coo(nglob, I, J, V, m->K);
+}
+
+// damageEvol.jl:5-7: W[:, :, damage_idx] .*= factor, then K is assembled again (the quasi-
+// static solver pieces are rebuilt on next use).
+void damage_evolve(orc_model* m) {
+    for (int64_t e : m->damage_el)
+        for (int q = 0; q < 25; ++q) m->W[(size_t)25 * e + q] *= m->damage_factor;
+    assemble_K(m);
+    m->qs_ready = false;
+    m->damage_count += 1;
+}
+
 void setup_model(orc_model* m) {
     const orc_config& c = m->cfg;
     const int NGLL = 5;
@@ -249,6 +296,13 @@ void setup_model(orc_model* m) {
                         mu[i][j] = mv;
                     }
             }
+            {   // element of the damage zone: the rectangle rule (Assemble.jl:34-35), or, for the
+                // per-node trapezoid, any node with the damaged material
+                bool in = false;
+                for (int j = 0; j < NGLL; ++j)
+                    for (int i = 0; i < NGLL; ++i) in = in || mu[i][j] != c.rho1 * (c.vs1 * c.vs1);
+                if (in && c.damage != 0) m->damage_idx.push_back(eo);
+            }
             for (int j = 0; j < NGLL; ++j)
                 for (int i = 0; i < NGLL; ++i) muMax = std::max(muMax, mu[i][j]);
             for (int j = 0; j < NGLL; ++j)
@@ -275,37 +329,7 @@ void setup_model(orc_model* m) {
     m->muMax = muMax;
 
     // ---- stiffness assembly (Kassemble.jl:3-63) ----
-    {
-        const double* H = m->H.data();
-        auto Hm = [&](int i, int j) { return H[i + NGLL * j]; };
-        const double cy = m->jac / (m->dy_deta * m->dy_deta);  // multiplies the eta terms
-        const double cx = m->jac / (m->dx_dxi * m->dx_dxi);
-        std::vector<int64_t> I, J;
-        vec V;
-        const size_t per = (size_t)NGLL * NGLL * (2 * NGLL - 1);
-        I.reserve(per * m->Nel);
-        J.reserve(per * m->Nel);
-        V.reserve(per * m->Nel);
-        for (int64_t eo = 0; eo < m->Nel; ++eo) {
-            const double* ww = &m->W[(int64_t)NGLL * NGLL * eo];
-            auto w = [&](int i, int j) { return ww[i + NGLL * j]; };
-            for (int l = 0; l < NGLL; ++l)
-                for (int k = 0; k < NGLL; ++k)
-                    for (int j = 0; j < NGLL; ++j)
-                        for (int i = 0; i < NGLL; ++i) {
-                            if (i != k && j != l) continue;
-                            double term1 = 0.0, term2 = 0.0;
-                            for (int p = 0; p < NGLL; ++p) {
-                                term1 += (i == k ? 1.0 : 0.0) * w(k, p) * cy * Hm(j, p) * Hm(l, p);
-                                term2 += (j == l ? 1.0 : 0.0) * w(p, j) * cx * Hm(i, p) * Hm(k, p);
-                            }
-                            I.push_back(IG(i, j, eo));
-                            J.push_back(IG(k, l, eo));
-                            V.push_back(term1 + term2);
-                        }
-        }
-        csr_from_coo(nglob, I, J, V, m->K);
-    }
+    assemble_K(m);
 
     // ---- time-step (par.jl:155-158) ----
     dt = c.CFL * dt;

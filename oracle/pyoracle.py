@@ -98,6 +98,9 @@ def lib() -> C.CDLL:
         L.orc_reset.argtypes = [P]
         L.orc_state.argtypes = [P, C.c_char_p, P]
         L.orc_set_state.argtypes = [P, C.c_char_p, P]
+        L.orc_set_damage.restype = I
+        L.orc_set_damage.argtypes = [P, C.POINTER(C.c_int64), I64, D]
+        L.orc_damage_evolve.argtypes = [P]
         L.orc_set_threads.argtypes = [I]
         L.orc_get_threads.restype = I
         _lib = L
@@ -131,7 +134,7 @@ def gll(ngll: int):
 
 
 _INT_ARRAYS = {"iglob", "iFlt", "iBcL", "iBcT", "FltIglobBC", "FltNI", "out_seis", "K_ptr", "K_col",
-               "regime", "cg_iters"}
+               "regime", "cg_iters", "damage_idx"}
 _COL_ARRAYS = {"seismic_stress", "seismic_slipvel", "seismic_slip", "is_stress", "is_slipvel", "is_slip",
                "taubefore", "tauafter", "delfafter"}
 _ROW_ARRAYS = {"dSeis", "vSeis", "aSeis"}
@@ -207,6 +210,15 @@ class Oracle:
             qs_maxit: int = 0) -> int:
         t_end = self.scalar("Total_time") if t_end is None else t_end
         return lib().orc_run(self.h, nsteps, t_end, qs_mode, qs_tol, qs_maxit)
+
+    def set_damage(self, idx, factor: float = 0.95):
+        """Elements (1-based) whose W is scaled by ``factor`` at every event end (damageEvol.jl)."""
+        a = np.ascontiguousarray(idx, dtype=np.int64)
+        if lib().orc_set_damage(self.h, a.ctypes.data_as(C.POINTER(C.c_int64)), len(a), float(factor)) != 0:
+            raise ValueError("damage element out of range")
+
+    def damage_evolve(self):
+        lib().orc_damage_evolve(self.h)
 
     def reset(self):
         lib().orc_reset(self.h)

@@ -159,3 +159,37 @@ def test_event_statistics_restatement():
     assert np.allclose(cat.recurrence, [100.0])
     c = compare(cat, cat)
     assert c["compared"] == 2 and c["recurrence"] == 0 and c["coseismic_slip"] == 0 and c["hypocentre_depth"] == 0
+
+
+@pytest.mark.parametrize("cfg", [reference_config(res=1), preset("dz40")], ids=["ref-res1", "dz40"])
+def test_damage_evolution_restatement(oracle_mod, cfg):
+    """damageEvol.jl in the oracle: the damage zone of Assemble.jl:25-35 (the host setup gives
+    the same elements), W of those elements scaled by the factor, K assembled again; the
+    assembled and the element-wise apply still agree, and K changes only through those
+    elements (K' x - K x = (f - 1) K_D x, K_D the damaged elements' part, which is zero for x
+    supported away from the damage zone)."""
+    from eqcycle_gb300 import set_parameters
+    P = set_parameters(cfg)
+    o = oracle_mod.Oracle(cfg)
+    di = o.get("damage_idx")
+    assert len(di) > 0 and np.array_equal(di, P.extra["damage_idx"])
+    W0 = o.get("W").copy()
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, o.nglob)
+    y0 = o.apply_K_csr(x)
+    o.set_damage(di, 0.95)
+    o.damage_evolve()
+    assert o.scalar("damage_count") == 1
+    W1 = o.get("W")
+    mask = np.zeros(W0.shape[2], bool)
+    mask[di - 1] = True
+    assert np.array_equal(W1[:, :, ~mask], W0[:, :, ~mask])
+    assert np.allclose(W1[:, :, mask], 0.95 * W0[:, :, mask], rtol=1e-15, atol=0)
+    y1 = o.apply_K_csr(x)
+    assert np.max(np.abs(y1 - o.apply_K_elem(x))) <= 1e-13 * np.max(np.abs(y1))
+    # nodes of undamaged elements only: K x unchanged there
+    ig = o.get("iglob") - 1
+    touched = np.zeros(o.nglob, bool)
+    touched[np.unique(ig[:, :, mask])] = True
+    assert np.array_equal(y1[~touched], y0[~touched])
+    assert np.max(np.abs(y1[touched] - y0[touched])) > 0
