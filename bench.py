@@ -401,6 +401,27 @@ def bench_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_setup(args):
+    """Model setup time on the workload mesh: the host setup (set_parameters over the whole mesh,
+    then eqc_create uploading iglob/W/M) against the setup on the device (structured_parameters
+    over the mesh edges, then eqc_create_structured building W, M, 1/M and diag K with kernels),
+    with eqc_create's phases; the multigrid hierarchy is built on the host in both."""
+    from eqcycle_gb300 import EQC_MIXED, Solver, preset, set_parameters, structured_parameters
+    cfg = preset(args.workload)
+    out = {"workload": args.workload}
+    for name, fn in (("host", set_parameters), ("device", structured_parameters)):
+        t0 = time.perf_counter()
+        P = fn(cfg)
+        t1 = time.perf_counter()
+        s = Solver(P, precision=EQC_MIXED)
+        t2 = time.perf_counter()
+        out[name] = {"parameters_s": t1 - t0, "create_s": t2 - t1, "total_s": t2 - t0,
+                     **{k: s.scalar(f"setup_ms_{k}") for k in ("numbering", "elements", "nodes", "other",
+                                                                 "hierarchy")}}
+        s.close()
+    print(json.dumps(out), flush=True)
+
+
 def bench_kernel(args):
     """Stiffness apply alone on the workload mesh, L2 flushed between launches."""
     from eqcycle_gb300 import EQC_PC_JACOBI, Solver, preset, set_parameters
@@ -583,6 +604,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true", help="time the stiffness apply alone")
+    ap.add_argument("--setup", action="store_true", help="time the model setup, host against device")
     ap.add_argument("--dtype", default="both", choices=["both", "f32", "f64"])
     ap.add_argument("--nrep", type=int, default=20)
     ap.add_argument("--learned", action="store_true", help="learned initial guess: train and evaluate")
@@ -605,6 +627,8 @@ def main():
         args.workload = "dz480"
     if args.kernel_only:
         bench_kernel(args)
+    elif args.setup:
+        bench_setup(args)
     elif args.learned:
         bench_learned(args)
     elif args.ensemble:

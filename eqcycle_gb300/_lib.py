@@ -42,6 +42,12 @@ class EqcModel(C.Structure):
     ]
 
 
+class EqcMaterial(C.Structure):
+    _fields_ = [("rule", C.c_int32), ("rho1", C.c_double), ("vs1", C.c_double), ("rho2", C.c_double),
+                ("vs2", C.c_double), ("ThickX", C.c_double), ("ThickY", C.c_double), ("trap_w0", C.c_double),
+                ("trap_w1", C.c_double), ("trap_z1", C.c_double), ("LX", C.c_double), ("xgll", _dp), ("wgll", _dp)]
+
+
 class EqcOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("precond", C.c_int32), ("guess", C.c_int32), ("tol_rule", C.c_int32),
                 ("cg_tol", C.c_double), ("cg_maxit", C.c_int32), ("device", C.c_int32),
@@ -66,7 +72,7 @@ _lib: Optional[C.CDLL] = None
 EXPORTS = ["eqc_default_options", "eqc_create", "eqc_destroy", "eqc_last_error", "eqc_apply_K", "eqc_qs_solve",
            "eqc_slrFunc", "eqc_FBC", "eqc_dtevol", "eqc_dtevol_noalloc", "eqc_init", "eqc_run", "eqc_get_state", "eqc_set_state",
            "eqc_get_scalar", "eqc_set_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
-           "eqc_time_apply", "eqc_launch_count", "eqc_sync", "eqc_set_damage", "eqc_damage_evolve", "eqc_guess_shape", "eqc_guess_init",
+           "eqc_time_apply", "eqc_launch_count", "eqc_sync", "eqc_set_damage", "eqc_damage_evolve", "eqc_create_structured", "eqc_guess_shape", "eqc_guess_init",
            "eqc_guess_get_params", "eqc_guess_set_params", "eqc_guess_log", "eqc_guess_pairs", "eqc_guess_train",
            "eqc_guess_eval", "eqc_guess_grad", "eqc_autotune", "eqc_ensemble_create", "eqc_ensemble_run",
            "eqc_ensemble_destroy", "eqc_ensemble_last_error"]
@@ -110,6 +116,8 @@ def lib() -> C.CDLL:
     L.eqc_sync.argtypes = [P]
     L.eqc_set_damage.argtypes = [P, C.POINTER(C.c_int64), C.c_int64, C.c_double]
     L.eqc_damage_evolve.argtypes = [P]
+    L.eqc_create_structured.argtypes = [C.POINTER(EqcModel), C.POINTER(EqcMaterial), C.POINTER(EqcOptions),
+                                        C.POINTER(P)]
     _fp = C.POINTER(C.c_float)
     U64 = C.c_uint64
     L.eqc_guess_shape.argtypes = [P, C.POINTER(I32), C.POINTER(I32), C.POINTER(I64)]

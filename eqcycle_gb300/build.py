@@ -26,7 +26,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
 # Translation units whose arithmetic mirrors the reference's operation order exactly
 # (friction Newton, state evolution): no FMA contraction.
-NO_FMAD = {"stepper.cu"}
+NO_FMAD = {"stepper.cu", "setup.cu"}
 
 
 def nvcc() -> str:

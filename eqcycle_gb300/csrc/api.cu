@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <chrono>
 
 namespace eqc {
 
@@ -101,12 +102,34 @@ void damage_evolve(Handle& h) {
     h.gen += 1;
 }
 
-static void create(Handle& h, const eqc_model& m) {
+// Reference node id (0-based) of lexicographic node (ix, iy) by MeshBox.jl:27-88's numbering:
+// a node gets its id from the first element (in element order) that contains it, in the order
+// that element creates its new nodes.
+static int64_t meshbox_id(int64_t ix, int64_t iy, int64_t nx) {
+    const int64_t exc = ix == 0 ? 0 : (ix - 1) / 4, i = ix - 4 * exc;
+    const int64_t eyc = iy == 0 ? 0 : (iy - 1) / 4, j = iy - 4 * eyc;
+    const int64_t rowstart = eyc == 0 ? 0 : 5 * nx + (eyc - 1) * 4 * nx;
+    if (eyc == 0 && exc == 0) return i + 5 * j;
+    if (eyc == 0) return 25 + 20 * (exc - 1) + (i - 1) + 4 * j;
+    if (exc == 0) return rowstart + i + 5 * (j - 1);
+    return rowstart + 20 + 16 * (exc - 1) + (i - 1) + 4 * (j - 1);
+}
+
+// mat == nullptr: the element data come from the caller (iglob, W, M of setParameters);
+// otherwise the mesh numbering is MeshBox's and W, M, 1/M and diag(K) are built on the device.
+static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     fail_if(m.NGLL != 5, "NGLL must be 5");
     fail_if(m.NelX < 1 || m.NelY < 1 || m.Nel != m.NelX * m.NelY, "Nel != NelX*NelY");
     fail_if(m.FltNglob != 4 * m.NelX + 1, "FltNglob != 4*NelX+1");
     fail_if(m.nglob != (4 * m.NelX + 1) * (4 * m.NelY + 1), "nglob != (4NelX+1)(4NelY+1)");
-    fail_if(!m.iglob || !m.W || !m.H || !m.M || !m.iFlt, "null model array");
+    fail_if(!m.H || !m.iFlt, "null model array");
+    if (mat) {
+        fail_if(!mat->xgll || !mat->wgll, "eqc_material needs the GLL nodes and weights");
+        fail_if(mat->rule < 0 || mat->rule > 2, "eqc_material.rule must be 0, 1 or 2");
+        fail_if(mat->rule == 2 && !(mat->trap_z1 > 0), "eqc_material.trap_z1 must be positive");
+    } else {
+        fail_if(!m.iglob || !m.W || !m.M, "null model array");
+    }
     fail_if(m.IDstate != 2, "only IDstate = 2 (aging law, log form) is on the hot path");
     fail_if(m.ETA != 0.0, "Kelvin-Voigt damping (ETA != 0) is not on the hot path");
     EQC_CUDA(cudaSetDevice(h.opt.device));
@@ -134,10 +157,17 @@ static void create(Handle& h, const eqc_model& m) {
     h.yr2sec = (double)m.yr2sec;
     std::memcpy(h.H, m.H, sizeof(h.H));
     set_H(h.H, s);
+    using clk = std::chrono::steady_clock;
+    auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+    auto t0 = clk::now();
 
-    // reference node -> layout index, from the connectivity
+    // reference node -> layout index, from the connectivity (or MeshBox's numbering rule)
     h.ref2lay.assign(m.nglob, -1);
-    for (int64_t e = 0; e < m.Nel; ++e) {
+    if (mat) {
+        for (int64_t iy = 0; iy < L.ny; ++iy)
+            for (int64_t ix = 0; ix < L.nx; ++ix) h.ref2lay[meshbox_id(ix, iy, L.nx)] = iy * L.ld + ix;
+    }
+    for (int64_t e = 0; e < (mat ? 0 : m.Nel); ++e) {
         const int ex = (int)(e % m.NelX), ey = (int)(e / m.NelX);
         for (int j = 0; j < 5; ++j)
             for (int i = 0; i < 5; ++i) {
@@ -153,19 +183,25 @@ static void create(Handle& h, const eqc_model& m) {
     for (int k = 0; k < Nf; ++k)
         fail_if(h.ref2lay[m.iFlt[k] - 1] != k, "iFlt must run along the y = 0 edge from x = -LX (BoundaryMatrix 'B')");
 
+    h.setup_ms[0] = ms_since(t0);   // node numbering
+    t0 = clk::now();
     // element data
-    load_element_data(h, m.W);
+    if (mat) setup_element_data_device(h, *mat);
+    else load_element_data(h, m.W);
+    EQC_CUDA(cudaStreamSynchronize(s));
+    h.setup_ms[1] = ms_since(t0);   // W and its copies (and diag K on the host path)
+    t0 = clk::now();
 
     // node arrays
     const int64_t N = L.size();
-    std::vector<double> Mlay(N, 1.0);
-    for (int64_t g = 0; g < m.nglob; ++g) Mlay[h.ref2lay[g]] = m.M[g];
     for (DBuf<double>* b : {&h.M, &h.d, &h.v, &h.a, &h.dPre, &h.tmp64a, &h.tmp64b, &h.tmp64c, &h.r64, &h.z64, &h.p64,
                              &h.q64, &h.Kd})
         b->alloc(N);
     for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32, &h.g32}) b->alloc(N);
-    h.M.upload(Mlay.data(), N, s);
-    {
+    if (!mat) {
+        std::vector<double> Mlay(N, 1.0);
+        for (int64_t g = 0; g < m.nglob; ++g) Mlay[h.ref2lay[g]] = m.M[g];
+        h.M.upload(Mlay.data(), N, s);
         std::vector<double> inv(N);
         for (int64_t i = 0; i < N; ++i) inv[i] = 1.0 / Mlay[i];
         h.invM.alloc(N);
@@ -204,6 +240,7 @@ static void create(Handle& h, const eqc_model& m) {
     h.nSeis = (int)m.n_out_seis;
     fail_if(h.nSeis > 32, "at most 32 receivers");
     h.seis.alloc(3 * std::max(h.nSeis, 1));
+    if (mat) setup_node_data_device(h, *mat, lBcL, m.BcLC, lBcT, m.BcTC);   // M (+ boundary terms), 1/M, diag K
 
     // fault arrays (fault order == layout row 0)
     FaultDev& F = h.F;
@@ -233,7 +270,12 @@ static void create(Handle& h, const eqc_model& m) {
     F.FltZ.upload(m.FltZ, Nf, s);
     F.FltX.upload(m.FltX, Nf, s);
     std::vector<double> Mf(Nf);
-    for (int k = 0; k < Nf; ++k) Mf[k] = m.M[m.iFlt[k] - 1];
+    if (mat) {   // fault order == layout row 0
+        h.M.download(Mf.data(), Nf, s);
+        EQC_CUDA(cudaStreamSynchronize(s));
+    } else {
+        for (int k = 0; k < Nf; ++k) Mf[k] = m.M[m.iFlt[k] - 1];
+    }
     F.Mf.upload(Mf.data(), Nf, s);
     F.creep.alloc(Nf);
     F.creep.upload(creep.data(), Nf, s);
@@ -242,6 +284,9 @@ static void create(Handle& h, const eqc_model& m) {
     h.h_tauo.assign(m.tauo, m.tauo + Nf);
     h.h_FltX.assign(m.FltX, m.FltX + Nf);
 
+    EQC_CUDA(cudaStreamSynchronize(s));
+    h.setup_ms[2] = ms_since(t0);   // node and fault arrays (M, 1/M; diag K on the device path)
+    t0 = clk::now();
     // control, reductions
     h.ctrl.alloc(1);
     EQC_CUDA(cudaStreamSynchronize(s));
@@ -262,7 +307,11 @@ static void create(Handle& h, const eqc_model& m) {
     }
     std::memset(h.h_cg, 0, sizeof(CGState));
     EQC_CUDA(cudaStreamSynchronize(s));
+    h.setup_ms[3] = ms_since(t0);
+    t0 = clk::now();
     if (h.opt.precond == EQC_PC_AMG) mg_build(h);
+    EQC_CUDA(cudaStreamSynchronize(s));
+    h.setup_ms[4] = ms_since(t0);   // multigrid hierarchy (host Galerkin products, device bounds)
 }
 
 static void to_layout(const Handle& h, const double* ref, std::vector<double>& lay) {
@@ -322,7 +371,29 @@ eqc_status eqc_create(const eqc_model* model, const eqc_options* opt, eqc_handle
     eqc_handle* H = new eqc_handle();
     if (opt) H->h.opt = *opt;
     else eqc_default_options(&H->h.opt);
-    eqc_status st = guarded(H, [&] { create(H->h, *model); });
+    eqc_status st = guarded(H, [&] { create(H->h, *model, nullptr); });
+    if (st != EQC_OK) {
+        g_create_err = H->h.err;
+        delete H;
+        return st;
+    }
+    *out = H;
+    return EQC_OK;
+}
+
+eqc_status eqc_create_structured(const eqc_model* model, const eqc_material* mat, const eqc_options* opt,
+                                 eqc_handle** out) {
+    if (!model || !mat || !out) return EQC_E_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_create_err = "no CUDA device";
+        return EQC_E_NOGPU;
+    }
+    eqc_handle* H = new eqc_handle();
+    if (opt) H->h.opt = *opt;
+    else eqc_default_options(&H->h.opt);
+    eqc_status st = guarded(H, [&] { create(H->h, *model, mat); });
     if (st != EQC_OK) {
         g_create_err = H->h.err;
         delete H;
@@ -467,6 +538,11 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         if (s == "t") *out = C.t;
         else if (s == "apply_variant") *out = h.opt.apply_variant;
         else if (s == "damage_events") *out = (double)h.damage_count;
+        else if (s == "setup_ms_numbering") *out = h.setup_ms[0];
+        else if (s == "setup_ms_elements") *out = h.setup_ms[1];
+        else if (s == "setup_ms_nodes") *out = h.setup_ms[2];
+        else if (s == "setup_ms_other") *out = h.setup_ms[3];
+        else if (s == "setup_ms_hierarchy") *out = h.setup_ms[4];
         else if (s == "reliable_delta") *out = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : 1e-3;
         else if (s == "dt") *out = C.dt;
         else if (s == "isolver") *out = C.isolver;

@@ -91,6 +91,7 @@ struct Handle {
     double damage_factor = 1.0;
     int64_t damage_count = 0;
     int64_t gen = 0;
+    double setup_ms[5] = {0, 0, 0, 0, 0};   // eqc_create phases: numbering, elements, nodes, other, hierarchy
     // Stream that work is enqueued on: the handle's own stream, or, while a conditional
     // body of a step graph is being captured, that body's capture stream.
     cudaStream_t stream = nullptr;
@@ -208,6 +209,9 @@ int64_t capture_tally();
 void init_state(Handle& h, double V_init);
 void destroy_graphs(Handle& h);
 void damage_evolve(Handle& h);
+void setup_element_data_device(Handle& h, const eqc_material& mat);
+void setup_node_data_device(Handle& h, const eqc_material& mat, const std::vector<int64_t>& lBcL, const double* BcLC,
+                            const std::vector<int64_t>& lBcT, const double* BcTC);
 // One whole time step of regime iso (1 quasi-static, 2 dynamic) on h.stream; graph: inside a capture.
 void enqueue_step(Handle& h, int iso, bool graph);
 // Host side of a finished step (control block already in h.h_ctrl): checks and outputs.

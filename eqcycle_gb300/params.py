@@ -193,6 +193,55 @@ def _mesh_numbering(NelX: int, NelY: int):
     return ids  # [iy, ix]
 
 
+def _fault_profiles(cfg: ModelConfig, FltX: np.ndarray, muMax: float, LX: float):
+    """Friction parameters and initial stress along the fault (defaultInitialConditions.jl, or the
+    workloads' uniform a / tapered b / seeded theta) and XiLf (par.jl:304-339)."""
+    Nf = len(FltX)
+    fo = np.full(Nf, cfg.fo)
+    Vo = np.full(Nf, cfg.Vo)
+    xLf = np.full(Nf, cfg.Dc)
+    if cfg.profile == 0:
+        X = FltX
+        z = np.abs(X)
+        ab = np.full(Nf, 0.015 - 0.019)
+        ab = np.where(z <= 2e3, _int1d(0.012, 0e3, -0.0041, -2e3, X), ab)
+        ab = np.where((z > 2e3) & (z <= 12e3), _int1d(-0.0041, -2e3, -0.0041, -12e3, X), ab)
+        ab = np.where((z > 12e3) & (z <= 17e3), _int1d(-0.0041, -12e3, 0.015, -17e3, X), ab)
+        ab = np.where((z > 17e3) & (z <= 24e3), _int1d(0.015, -17e3, 0.024, -24e3, X), ab)
+        ab = np.where(z > 24e3, 0.0047, ab)
+        ccb = np.full(Nf, 0.019)
+        cca = ccb + ab
+        Seff = np.where(z <= 2e3, _int1d(10e6, 0, 50e6, -2e3, X), 50e6)
+        t0 = np.full(Nf, 22.5e6)
+        t0 = np.where(z <= 2e3, _int1d(0.01e6, 0, 30e6, -2e3, X), t0)
+        t0 = np.where((z > 2e3) & (z <= 12e3), _int1d(30e6, -2e3, 30e6, -12e3, X), t0)
+        t0 = np.where((z > 12e3) & (z <= 17e3), _int1d(30e6, -12e3, 22.5e6, -17e3, X), t0)
+        t0 = np.where((z > 17e3) & (z <= 24e3), _int1d(22.5e6, -17e3, 22.5e6, -24e3, X), t0)
+        tauo = t0
+    else:
+        z = np.abs(FltX)
+        b = np.where(z <= cfg.zb0, cfg.b0,
+                     np.where(z >= cfg.zb1, cfg.b1, cfg.b0 + (cfg.b1 - cfg.b0) * ((z - cfg.zb0) / (cfg.zb1 - cfg.zb0))))
+        cca = np.full(Nf, cfg.a0)
+        ccb = b.astype(np.float64)
+        Seff = np.full(Nf, cfg.sigma)
+        u = splitmix_uniform_pm1(cfg.seed, Nf)
+        theta = (cfg.Dc / cfg.Vpl) * (1.0 + cfg.noise_amp * u)
+        psi0 = np.log(cfg.Vo * theta / cfg.Dc)
+        tauo = Seff * (cfg.fo + ccb * psi0 + cca * np.log(cfg.V_init / cfg.Vo))
+
+    # ---- XiLf (par.jl:304-339) ----
+    hcell = LX / (Nf - 1)
+    gamma_ = math.pi / 4.0
+    expr1 = -(cca - ccb) / cca
+    expr2 = gamma_ * muMax / hcell * xLf / (cca * Seff)
+    ro = expr2 - expr1
+    Xith = np.where(0.25 * ro * ro - expr2 >= 0, 1.0 / ro, 1.0 - expr1 / expr2)
+    XiLf = np.where(1.0 * Xith > 0.5, 0.5 * xLf, 1.0 * Xith * xLf)
+
+    return fo, Vo, xLf, cca, ccb, Seff, tauo, XiLf
+
+
 def set_parameters(cfg: ModelConfig) -> Params:
     """Build the model of ``cfg`` exactly as par.jl:setParameters does."""
     NGLL = 5
@@ -314,49 +363,8 @@ def set_parameters(cfg: ModelConfig) -> Params:
     FltZ = ((M[iFlt] / FltB) / half_dt) * 0.5
     FltX = x[iFlt]
 
-    # ---- friction and profiles ----
-    Nf = FltNglob
-    fo = np.full(Nf, cfg.fo)
-    Vo = np.full(Nf, cfg.Vo)
-    xLf = np.full(Nf, cfg.Dc)
-    if cfg.profile == 0:
-        X = FltX
-        z = np.abs(X)
-        ab = np.full(Nf, 0.015 - 0.019)
-        ab = np.where(z <= 2e3, _int1d(0.012, 0e3, -0.0041, -2e3, X), ab)
-        ab = np.where((z > 2e3) & (z <= 12e3), _int1d(-0.0041, -2e3, -0.0041, -12e3, X), ab)
-        ab = np.where((z > 12e3) & (z <= 17e3), _int1d(-0.0041, -12e3, 0.015, -17e3, X), ab)
-        ab = np.where((z > 17e3) & (z <= 24e3), _int1d(0.015, -17e3, 0.024, -24e3, X), ab)
-        ab = np.where(z > 24e3, 0.0047, ab)
-        ccb = np.full(Nf, 0.019)
-        cca = ccb + ab
-        Seff = np.where(z <= 2e3, _int1d(10e6, 0, 50e6, -2e3, X), 50e6)
-        t0 = np.full(Nf, 22.5e6)
-        t0 = np.where(z <= 2e3, _int1d(0.01e6, 0, 30e6, -2e3, X), t0)
-        t0 = np.where((z > 2e3) & (z <= 12e3), _int1d(30e6, -2e3, 30e6, -12e3, X), t0)
-        t0 = np.where((z > 12e3) & (z <= 17e3), _int1d(30e6, -12e3, 22.5e6, -17e3, X), t0)
-        t0 = np.where((z > 17e3) & (z <= 24e3), _int1d(22.5e6, -17e3, 22.5e6, -24e3, X), t0)
-        tauo = t0
-    else:
-        z = np.abs(FltX)
-        b = np.where(z <= cfg.zb0, cfg.b0,
-                     np.where(z >= cfg.zb1, cfg.b1, cfg.b0 + (cfg.b1 - cfg.b0) * ((z - cfg.zb0) / (cfg.zb1 - cfg.zb0))))
-        cca = np.full(Nf, cfg.a0)
-        ccb = b.astype(np.float64)
-        Seff = np.full(Nf, cfg.sigma)
-        u = splitmix_uniform_pm1(cfg.seed, Nf)
-        theta = (cfg.Dc / cfg.Vpl) * (1.0 + cfg.noise_amp * u)
-        psi0 = np.log(cfg.Vo * theta / cfg.Dc)
-        tauo = Seff * (cfg.fo + ccb * psi0 + cca * np.log(cfg.V_init / cfg.Vo))
-
-    # ---- XiLf (par.jl:304-339) ----
-    hcell = LX / (Nf - 1)
-    gamma_ = math.pi / 4.0
-    expr1 = -(cca - ccb) / cca
-    expr2 = gamma_ * muMax / hcell * xLf / (cca * Seff)
-    ro = expr2 - expr1
-    Xith = np.where(0.25 * ro * ro - expr2 >= 0, 1.0 / ro, 1.0 - expr1 / expr2)
-    XiLf = np.where(1.0 * Xith > 0.5, 0.5 * xLf, 1.0 * Xith * xLf)
+    # ---- friction and profiles, XiLf ----
+    fo, Vo, xLf, cca, ccb, Seff, tauo, XiLf = _fault_profiles(cfg, FltX, muMax, LX)
 
     # ---- FltNI, FltIglobBC, receivers ----
     mask = np.ones(nglob, dtype=bool)
@@ -385,4 +393,164 @@ def set_parameters(cfg: ModelConfig) -> Params:
         mesh=Mesh(NelX, NelY, NGLL, dxe, dye, iglob, W, H, xgll, wgll, x, y, muMax),
         cfg=cfg,
         extra={"damage_idx": damage_idx},
+    )
+
+
+# --------------------------------------------------------------------------- structured setup
+def meshbox_ids(ix, iy, nx: int):
+    """Reference node id (0-based) of lexicographic nodes (ix, iy) by MeshBox.jl's numbering
+    (the rule of ``_mesh_numbering``, for given nodes only)."""
+    ix = np.asarray(ix, dtype=np.int64)
+    iy = np.asarray(iy, dtype=np.int64)
+    exc = np.where(ix == 0, 0, (ix - 1) // 4)
+    i = ix - 4 * exc
+    eyc = np.where(iy == 0, 0, (iy - 1) // 4)
+    j = iy - 4 * eyc
+    rowstart = np.where(eyc == 0, 0, 5 * nx + (eyc - 1) * 4 * nx)
+    return np.where((eyc == 0) & (exc == 0), i + 5 * j,
+           np.where(eyc == 0, 25 + 20 * (exc - 1) + (i - 1) + 4 * j,
+           np.where(exc == 0, rowstart + i + 5 * (j - 1),
+                    rowstart + 20 + 16 * (exc - 1) + (i - 1) + 4 * (j - 1))))
+
+
+def structured_parameters(cfg: ModelConfig) -> Params:
+    """The parameters of ``cfg`` without the per-node and per-element arrays (iglob, W, M,
+    FltNI, coordinates), for ``eqc_create_structured``, which builds those on the device.  Every
+    array it returns is bitwise the one ``set_parameters`` returns; it touches O(NelX + NelY)
+    nodes instead of O(nglob)."""
+    NGLL = 5
+    NelX, NelY = int(cfg.NelX), int(cfg.NelY)
+    LX, LY = float(cfg.LX), float(cfg.LY)
+    dxe, dye = LX / NelX, LY / NelY
+    Nel = NelX * NelY
+    FltNglob = NelX * (NGLL - 1) + 1
+    dx_dxi, dy_deta = 0.5 * dxe, 0.5 * dye
+    jac = dx_dxi * dy_deta
+    Total_time = cfg.total_years * YR2SEC
+    xgll, wgll, H = gll(NGLL)
+    nx, ny = 4 * NelX + 1, 4 * NelY + 1
+    nglob = nx * ny
+    # axis coordinates (the last element writing a node defines it, MeshBox.jl)
+    ixs, iys = np.arange(nx), np.arange(ny)
+    exw = np.minimum(ixs // 4, NelX - 1)
+    eyw = np.minimum(iys // 4, NelY - 1)
+    X = (dxe * exw.astype(np.float64) + dxe * (0.5 * (1.0 + xgll[ixs - 4 * exw]))) - LX
+    Y = dye * eyw.astype(np.float64) + dye * (0.5 * (1.0 + xgll[iys - 4 * eyw]))
+    mu1, mu2 = cfg.rho1 * (cfg.vs1 * cfg.vs1), cfg.rho2 * (cfg.vs2 * cfg.vs2)
+
+    def element_rho(ex, ey):
+        """rho of elements under the rectangle rule (Assemble.jl:34-35) or the homogeneous one."""
+        if cfg.damage == 1:
+            dm = ((ex + 1) * dxe >= cfg.ThickX) & ((dye <= (ey + 1) * dye) & ((ey + 1) * dye <= cfg.ThickY))
+        else:
+            dm = np.zeros(np.shape(ex), dtype=bool)
+        return np.where(dm, cfg.rho2, cfg.rho1)
+
+    def trap(ix, iy):
+        z = -X[ix]
+        wdt = cfg.trap_w0 + (cfg.trap_w1 - cfg.trap_w0) * (z / cfg.trap_z1)
+        return (z <= cfg.trap_z1) & (Y[iy] <= wdt)
+
+    # damage zone elements, muMax, CFL time step
+    if cfg.damage == 1:
+        ex_ok = (np.arange(1, NelX + 1) * dxe >= cfg.ThickX)
+        ey_ok = (dye <= np.arange(1, NelY + 1) * dye) & (np.arange(1, NelY + 1) * dye <= cfg.ThickY)
+        dmg_el = (ey_ok[:, None] & ex_ok[None, :]).reshape(-1)
+        damage_idx = np.nonzero(dmg_el)[0] + 1
+        present = [(cfg.rho1, mu1)] + ([(cfg.rho2, mu2)] if dmg_el.any() else [])
+        if dmg_el.all():
+            present = [(cfg.rho2, mu2)]
+    elif cfg.damage == 2:
+        # damaged nodes lie within the widest width of the trapezoid from the fault
+        wmax = max(cfg.trap_w0, cfg.trap_w1, 0.0)
+        iy_max = int(np.nonzero(Y <= wmax)[0][-1]) if np.any(Y <= wmax) else 0
+        ey_max = min(iy_max // 4, NelY - 1)
+        hit = np.zeros((ey_max + 1, NelX), dtype=bool)
+        for j in range(5):
+            for i in range(5):
+                ixe = 4 * np.arange(NelX) + i
+                iye = 4 * np.arange(ey_max + 1) + j
+                hit |= trap(ixe[None, :], iye[:, None])
+        damage_idx = np.nonzero(hit.reshape(-1))[0] + 1      # e = ey*NelX + ex for ey <= ey_max
+        present = [(cfg.rho1, mu1)] + ([(cfg.rho2, mu2)] if hit.any() else [])
+    else:
+        damage_idx = np.zeros(0, dtype=np.int64)
+        present = [(cfg.rho1, mu1)]
+    damage_idx = damage_idx.astype(np.int64)
+    muMax = float(max(m for _, m in present))
+    vmax = max(float(np.sqrt(m / r)) for r, m in present)
+    dxg = np.diff(xgll)
+    h = dxe if dxe < dye else dye
+    dt = float(np.min((dxg * 0.5 * h) / vmax))
+    dt = cfg.CFL * dt
+    half_dt = 0.5 * dt
+
+    # boundary matrices (BoundaryMatrix.jl) with MeshBox ids of their nodes
+    def boundary(side):
+        if side == "L":
+            ne, jac1D, imp = NelY, dy_deta, cfg.rho1 * cfg.vs1
+            ixn, iyn = np.zeros(4 * ne + 1, np.int64), np.arange(4 * ne + 1)
+        elif side == "T":
+            ne, jac1D, imp = NelX, dx_dxi, cfg.rho1 * cfg.vs1
+            ixn, iyn = np.arange(4 * ne + 1), np.full(4 * ne + 1, ny - 1)
+        else:
+            ne, jac1D, imp = NelX, dx_dxi, 1.0
+            ixn, iyn = np.arange(4 * ne + 1), np.zeros(4 * ne + 1, np.int64)
+        B = np.zeros(4 * ne + 1)
+        contrib = (jac1D * wgll) * imp
+        for k in range(5):
+            np.add.at(B, 4 * np.arange(ne) + k, contrib[k])
+        return B, meshbox_ids(ixn, iyn, nx), ixn, iyn
+
+    BcLC, iBcL, _, _ = boundary("L")
+    BcTC, iBcT, _, _ = boundary("T")
+    FltB, iFlt, fix, _ = boundary("B")
+    # M at the fault nodes: element row 0's contributions in element order, then the boundary terms
+    Mf = np.zeros(FltNglob)
+    for ex in range(NelX):
+        i = np.arange(5)
+        ix = 4 * ex + i
+        if cfg.damage == 2:
+            rho = np.where(trap(ix, np.zeros(5, np.int64)), cfg.rho2, cfg.rho1)
+        else:
+            rho = element_rho(np.full(5, ex), np.zeros(5, np.int64))
+        np.add.at(Mf, ix, ((wgll * wgll[0]) * rho) * jac)
+    Mf[0] = Mf[0] + half_dt * BcLC[0]               # node (0, 0) is the left boundary's first
+    FltZ = ((Mf / FltB) / half_dt) * 0.5
+    FltX = X[fix]
+    fo, Vo, xLf, cca, ccb, Seff, tauo, XiLf = _fault_profiles(cfg, FltX, muMax, LX)
+
+    # creeping nodes (main.jl:185) and receivers (nearest node, smallest reference id on ties)
+    creeps = (np.abs(FltX) >= cfg.creep_depth) if cfg.creep_inclusive else (np.abs(FltX) > cfg.creep_depth)
+    FltIglobBC = np.zeros(0, dtype=np.int64)
+    if creeps.any():
+        last = iFlt[np.nonzero(creeps)[0][-1]]
+        fbc = meshbox_ids((4 * np.arange(NelX)[:, None] + np.arange(5)[None, :]).reshape(-1),
+                          np.zeros(5 * NelX, np.int64), nx)
+        idx = int(np.nonzero(fbc == last)[0][0])
+        FltIglobBC = fbc[: idx + 1].astype(np.int64)
+    out, rx, ry = [], [], []
+    for xr, yr in zip(cfg.rec_x, cfg.rec_y):
+        dx2, dy2 = (X - xr) ** 2, (Y - yr) ** 2
+        dmin = np.min(dx2 + np.min(dy2))       # the sum is monotonic in each term
+        best = None
+        for ix in np.nonzero(dx2 + np.min(dy2) == dmin)[0]:
+            for iy in np.nonzero(dx2[ix] + dy2 == dmin)[0]:
+                g = int(meshbox_ids(ix, iy, nx))
+                if best is None or g < best[0]:
+                    best = (g, ix, iy)
+        out.append(best[0])
+        rx.append(X[best[1]])
+        ry.append(Y[best[2]])
+    out_seis = np.array(out, dtype=np.int64)
+
+    return Params(
+        int_=ParamsInt(Nel, FltNglob, YR2SEC, Total_time, 2, nglob),
+        float_=ParamsFloat(0.0, cfg.Vpl, cfg.Vthres, cfg.Vthres, dt),
+        farray=ParamsFarray(fo, Vo, xLf, None, BcLC, BcTC, FltB, FltZ, FltX, cca, ccb, Seff, tauo, XiLf,
+                            np.array(rx), np.array(ry)),
+        iarray=ParamsIarray(iFlt + 1, iBcL + 1, iBcT + 1, FltIglobBC + 1, None, out_seis + 1),
+        mesh=Mesh(NelX, NelY, NGLL, dxe, dye, None, None, H, xgll, wgll, None, None, muMax),
+        cfg=cfg,
+        extra={"damage_idx": damage_idx, "structured": True, "Mf": Mf},
     )

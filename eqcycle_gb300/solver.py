@@ -77,16 +77,21 @@ class Solver:
         mod.ETA, mod.Vpl, mod.Vthres, mod.Vevne, mod.dt0 = (P.float_.ETA, P.float_.Vpl, P.float_.Vthres,
                                                           P.float_.Vevne, P.float_.dt0)
         mod.NelX, mod.NelY, mod.NGLL, mod.dxe, mod.dye = m.NelX, m.NelY, m.NGLL, m.dxe, m.dye
-        mod.iglob = i("iglob", np.asarray(m.iglob).reshape(-1, order="F"))
-        mod.W = d("W", np.asarray(m.W).reshape(-1, order="F"))
+        structured = bool(P.extra.get("structured"))   # element data built on the device
+        if not structured:
+            mod.iglob = i("iglob", np.asarray(m.iglob).reshape(-1, order="F"))
+            mod.W = d("W", np.asarray(m.W).reshape(-1, order="F"))
         mod.H = d("H", np.asarray(m.H).reshape(-1, order="F"))
         for name in ("fo", "Vo", "xLf", "M", "BcLC", "BcTC", "FltB", "FltZ", "FltX", "cca", "ccb", "Seff", "tauo",
                      "XiLf"):
-            setattr(mod, name, d(name, getattr(fa, name)))
+            if getattr(fa, name) is not None:
+                setattr(mod, name, d(name, getattr(fa, name)))
         for name in ("iFlt", "iBcL", "iBcT", "FltIglobBC", "FltNI", "out_seis"):
-            setattr(mod, name, i(name, getattr(ia, name)))
+            if getattr(ia, name) is not None:
+                setattr(mod, name, i(name, getattr(ia, name)))
         mod.n_iBcL, mod.n_iBcT = len(ia.iBcL), len(ia.iBcT)
-        mod.n_FltIglobBC, mod.n_FltNI, mod.n_out_seis = len(ia.FltIglobBC), len(ia.FltNI), len(ia.out_seis)
+        mod.n_FltIglobBC, mod.n_out_seis = len(ia.FltIglobBC), len(ia.out_seis)
+        mod.n_FltNI = 0 if ia.FltNI is None else len(ia.FltNI)
         self.options = L.default_options(precision=precision, precond=precond, guess=guess, cg_tol=cg_tol,
                                          cg_maxit=cg_maxit, tol_rule=tol_rule, device=device,
                                          use_graphs=use_graphs, verbose=verbose, reliable_delta=reliable_delta,
@@ -94,7 +99,14 @@ class Solver:
                                          mg_cluster_max=mg_cluster_max, apply_variant=apply_variant,
                                          mg_degree_coarse=mg_degree_coarse, step_batch=step_batch)
         h = C.c_void_p()
-        L.check(lib.eqc_create(C.byref(mod), C.byref(self.options), C.byref(h)), None)
+        if structured:
+            cfg = P.cfg
+            mat = L.EqcMaterial(rule=int(cfg.damage), rho1=cfg.rho1, vs1=cfg.vs1, rho2=cfg.rho2, vs2=cfg.vs2,
+                                ThickX=cfg.ThickX, ThickY=cfg.ThickY, trap_w0=cfg.trap_w0, trap_w1=cfg.trap_w1,
+                                trap_z1=cfg.trap_z1, LX=float(cfg.LX), xgll=d("xgll", m.xgll), wgll=d("wgll", m.wgll))
+            L.check(lib.eqc_create_structured(C.byref(mod), C.byref(mat), C.byref(self.options), C.byref(h)), None)
+        else:
+            L.check(lib.eqc_create(C.byref(mod), C.byref(self.options), C.byref(h)), None)
         self.h = h
         self.nglob = P.int_.nglob
         self.Nf = P.int_.FltNglob

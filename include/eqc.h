@@ -115,6 +115,31 @@ void eqc_default_options(eqc_options* opt);
 /* Uploads the model, builds the device layout and the multigrid hierarchy
  * (src/main.jl:193-211 builds its AMG once per run as well). */
 eqc_status eqc_create(const eqc_model* model, const eqc_options* opt, eqc_handle** out);
+
+/* Material of a structured box model, for the setup on the device (no counterpart in the
+ * reference, whose setParameters builds W and M on the host, par.jl:99-152). */
+typedef struct {
+    int32_t rule;                  /* 0 homogeneous (rho1, vs1); 1 rectangle per element
+                                      (Assemble.jl:34-35: ex*dxe >= ThickX and dye <= ey*dye
+                                      <= ThickY, 1-based ex, ey); 2 trapezoid per GLL node:
+                                      depth z = -x <= trap_z1 and y <= trap_w0 + (trap_w1 -
+                                      trap_w0) z / trap_z1                                 */
+    double rho1, vs1, rho2, vs2;   /* host rock; damage zone                               */
+    double ThickX, ThickY;         /* rule 1                                                */
+    double trap_w0, trap_w1, trap_z1;   /* rule 2                                           */
+    double LX;                     /* domain depth: x runs from -LX to 0                    */
+    const double* xgll;            /* the 5 GLL nodes and weights (as the host setup uses)  */
+    const double* wgll;
+} eqc_material;
+
+/* eqc_create for a structured box mesh whose element data are built on the device: the node
+ * numbering is MeshBox.jl's (model->iglob is not read), W, the lumped mass M with the
+ * absorbing-boundary terms M[iB] += dt0/2 * Bc of par.jl:173-174, 1/M and diag(K) are
+ * computed by kernels from `mat` (model->W, model->M and model->FltNI are not read; every other
+ * field is, as in eqc_create).  The result is bitwise the model eqc_create builds from the
+ * host setup's arrays. */
+eqc_status eqc_create_structured(const eqc_model* model, const eqc_material* mat, const eqc_options* opt,
+                                 eqc_handle** out);
 eqc_status eqc_destroy(eqc_handle* h);
 const char* eqc_last_error(const eqc_handle* h);
 
@@ -230,7 +255,9 @@ eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
  * increments judged against the previous-step guess / kept because they lowered ||r||),
  * "cg_restarts" (mixed precision: reliable updates after which the CG direction restarted),
  * the solver settings "apply_variant" and "reliable_delta" (as chosen by eqc_autotune), and
- * "damage_events" (damage steps applied, eqc_set_damage)).
+ * "damage_events" (damage steps applied, eqc_set_damage), and the host time in ms of the
+ * phases of eqc_create: "setup_ms_numbering", "setup_ms_elements", "setup_ms_nodes",
+ * "setup_ms_other", "setup_ms_hierarchy" (the multigrid hierarchy)).
  * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);

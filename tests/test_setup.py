@@ -39,3 +39,23 @@ def test_gll_symmetry():
     x, w, H = gll(5)
     assert np.allclose(x, -x[::-1], atol=0) and np.allclose(w, w[::-1], atol=0)
     assert np.allclose(H, -H[::-1, ::-1], atol=1e-13)
+
+
+@pytest.mark.parametrize("name", ["homog48", "dz40", "ref-res1", "ref-res2", "ens"])
+def test_structured_parameters_equal_the_full_setup(name):
+    """structured_parameters (the host part of the setup on the device: O(NelX + NelY) nodes)
+    returns bitwise the arrays set_parameters builds over the whole mesh."""
+    from eqcycle_gb300 import set_parameters, structured_parameters
+    from eqcycle_gb300.config import ensemble_members, preset, reference_config
+    cfg = {"homog48": preset("homog48"), "dz40": preset("dz40"), "ref-res1": reference_config(res=1),
+           "ref-res2": reference_config(res=2), "ens": ensemble_members(4)[3]}[name]
+    A, B = set_parameters(cfg), structured_parameters(cfg)
+    for f in ("fo", "Vo", "xLf", "BcLC", "BcTC", "FltB", "FltZ", "FltX", "cca", "ccb", "Seff", "tauo", "XiLf",
+              "xout", "yout"):
+        assert np.array_equal(getattr(A.farray, f), getattr(B.farray, f)), f
+    for f in ("iFlt", "iBcL", "iBcT", "FltIglobBC", "out_seis"):
+        assert np.array_equal(getattr(A.iarray, f), getattr(B.iarray, f)), f
+    assert A.float_.dt0 == B.float_.dt0 and A.mesh.muMax == B.mesh.muMax
+    assert np.array_equal(A.extra["damage_idx"], B.extra["damage_idx"])
+    assert np.array_equal(A.farray.M[A.iarray.iFlt - 1], B.extra["Mf"])
+    assert B.mesh.W is None and B.farray.M is None and B.iarray.FltNI is None
