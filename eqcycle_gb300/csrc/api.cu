@@ -4,6 +4,7 @@
 #include "learn.h"
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <algorithm>
 #include <chrono>
 
@@ -133,6 +134,7 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     fail_if(m.IDstate != 2, "only IDstate = 2 (aging law, log form) is on the hot path");
     fail_if(m.ETA != 0.0, "Kelvin-Voigt damping (ETA != 0) is not on the hot path");
     EQC_CUDA(cudaSetDevice(h.opt.device));
+    h.fuse = std::getenv("EQC_NO_FUSE") == nullptr;
     EQC_CUDA(cudaStreamCreateWithFlags(&h.own_stream, cudaStreamNonBlocking));
     h.stream = h.own_stream;
     cudaStream_t s = h.stream;

@@ -15,6 +15,7 @@
 // shared memory.
 #include "model.h"
 #include "vec.cuh"
+#include "epi.cuh"
 #include <cstdlib>
 #include <type_traits>
 #include <algorithm>
@@ -537,7 +538,8 @@ __device__ __forceinline__ void rows_lines(const float (&u)[5][5], const float (
 
 template <int ROWS, int MINB>
 __global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const float* __restrict__ x, float* __restrict__ y,
-                                                                     ApplyArgs<float> A, float sign, int zero_row0) {
+                                                                     ApplyArgs<float> A, float sign, int zero_row0,
+                                                                     OpEpi<float> E) {
     const Layout L = A.L;
     __shared__ float Ts[ROWS + 1][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -600,8 +602,8 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const floa
         const int iy = 4 * ey + j;
         if (iy >= L.ny) break;
         const float z = (zero_row0 && iy == 0) ? 0.f : sign;
-        *reinterpret_cast<float4*>(y + (int64_t)iy * L.ld + 4 * ex) =
-            make_float4(z * out[j][0], z * out[j][1], z * out[j][2], z * out[j][3]);
+        epi_store4(E, y, (int64_t)iy * L.ld + 4 * ex,
+                   make_float4(z * out[j][0], z * out[j][1], z * out[j][2], z * out[j][3]));
     }
 }
 
@@ -636,7 +638,7 @@ __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.p
 __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_constant__ CUtensorMap umap,
                                                                 const __grid_constant__ CUtensorMap wmap,
                                                                 float* __restrict__ y, ApplyArgs<float> A, float sign,
-                                                                int zero_row0, int nsx, int rw) {
+                                                                int zero_row0, int nsx, int rw, OpEpi<float> E) {
     extern __shared__ __align__(128) unsigned char smem[];
     const Layout L = A.L;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -750,8 +752,8 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
             const int iy = 4 * ey + j;
             if (iy >= L.ny) break;
             const float z = (zero_row0 && iy == 0) ? 0.f : sign;
-            *reinterpret_cast<float4*>(y + (int64_t)iy * L.ld + 4 * ex) =
-                make_float4(z * out[j][0], z * out[j][1], z * out[j][2], z * out[j][3]);
+            epi_store4(E, y, (int64_t)iy * L.ld + 4 * ex,
+                       make_float4(z * out[j][0], z * out[j][1], z * out[j][2], z * out[j][3]));
         }
     }
 }
@@ -899,13 +901,14 @@ static void walk_shape(const Layout& L, int* nsx, int* rw, int* nblk) {
     *nblk = *nsx * (int)((rows + r - 1) / r);
 }
 
-static bool launch_walk(const float* x, float* y, const ApplyArgs<float>& A, float sign, int zr, cudaStream_t s) {
+static bool launch_walk(const float* x, float* y, const ApplyArgs<float>& A, float sign, int zr, cudaStream_t s,
+                        const OpEpi<float>& E = OpEpi<float>()) {
     if (!A.tma || !A.tma->walk_ok || g_walk_slots <= 0) return false;
     const CUtensorMap* um = tma_umap_walk(*A.tma, x, A.L);
     if (!um) return false;
     int nsx, rw, nblk;
     walk_shape(A.L, &nsx, &rw, &nblk);
-    k_apply_walk<<<nblk, 32 * WK_ROWS, WK_BYTES, s>>>(*um, A.tma->w32walk, y, A, sign, zr, nsx, rw);
+    k_apply_walk<<<nblk, 32 * WK_ROWS, WK_BYTES, s>>>(*um, A.tma->w32walk, y, A, sign, zr, nsx, rw, E);
     EQC_CHECK_LAUNCH();
     count_launch();
     return true;
@@ -929,12 +932,13 @@ void set_H(const double* H, cudaStream_t s) {
 }
 
 // Element-per-lane apply: variant 0 -> 6 element rows per CTA (default), 4..7 -> 4, 6, 8, 12.
-static void launch_rows(const float* x, float* y, const ApplyArgs<float>& A, float sign, int zr, cudaStream_t s) {
+static void launch_rows(const float* x, float* y, const ApplyArgs<float>& A, float sign, int zr, cudaStream_t s,
+                        const OpEpi<float>& E = OpEpi<float>()) {
     const int sx = (A.L.NelX + 1 + 30) / 31;
     auto go = [&](auto rows_tag, auto minb_tag) {
         constexpr int R = decltype(rows_tag)::value, M = decltype(minb_tag)::value;
         dim3 g(sx, (A.L.NelY + 1 + R - 1) / R);
-        k_apply_rows<R, M><<<g, 32 * (R + 1), 0, s>>>(x, y, A, sign, zr);
+        k_apply_rows<R, M><<<g, 32 * (R + 1), 0, s>>>(x, y, A, sign, zr, E);
     };
     using I = std::integral_constant<int, 0>;
     (void)sizeof(I);
@@ -981,6 +985,16 @@ void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStre
     k_apply<T, TEX, TEY><<<grid, 256, sm, s>>>(x, y, A, sign, mode);
     EQC_CHECK_LAUNCH();
     count_launch();
+}
+
+bool apply_K_epi(const float* x, const ApplyArgs<float>& A, int mode, const OpEpi<float>& E, cudaStream_t s) {
+    if (mode > 1 || !A.Wp || !aligned16(x)) return false;
+    if (A.variant == 8 && launch_walk(x, nullptr, A, 1.0f, mode, s, E)) return true;
+    if (A.variant == 0 || (A.variant >= 4 && A.variant <= 7)) {
+        launch_rows(x, nullptr, A, 1.0f, mode, s, E);
+        return true;
+    }
+    return false;
 }
 
 template void apply_K<double>(const double*, double*, const ApplyArgs<double>&, double, int, cudaStream_t);

@@ -1,14 +1,17 @@
 // Multigrid V-cycle on the device (see mg.h for the hierarchy).
 #include "mg.h"
 #include "reduce.cuh"
+#include "epi.cuh"
 #include <cmath>
 #include <random>
+#include <utility>
 
 namespace eqc {
 
 // ------------------------------------------------------------------ device kernels
 template <class T>
-__global__ void k_stencil(const T* __restrict__ A, const T* __restrict__ x, T* __restrict__ y, int cx, int cy) {
+__global__ void k_stencil(const T* __restrict__ A, const T* __restrict__ x, T* __restrict__ y, int cx, int cy,
+                          OpEpi<T> E) {
     const int64_t N = (int64_t)cx * cy;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % cx), iy = (int)(i / cx);
@@ -20,7 +23,7 @@ __global__ void k_stencil(const T* __restrict__ A, const T* __restrict__ x, T* _
                 if (gx >= 0 && gx < cx && gy >= 1 && gy < cy) s += A[k * N + i] * x[(int64_t)gy * cx + gx];
             }
         }
-        y[i] = s;
+        epi_store1(E, y, i, s);
     }
 }
 
@@ -49,11 +52,30 @@ __global__ void k_prolong_add(const T* __restrict__ xc, T* __restrict__ xf, int 
     }
 }
 
+// The coarse level's first Chebyshev step from x = 0, fused into the restriction that produces
+// its right-hand side (k_cheb_first with with_x = 0): r = Dinv b ; d = r / theta ; x = d.
+template <class T>
+struct ChebFirst {
+    const T* dinv = nullptr;   // null: not fused
+    T *x = nullptr, *r = nullptr, *d = nullptr;
+    T inv_theta = T(0);
+};
+template <class T>
+__device__ __forceinline__ void cheb_first_pt(const ChebFirst<T>& F, int64_t i, T b) {
+    if (!F.dinv) return;
+    const T ri = mul_rn<T>(F.dinv[i], b);
+    const T di = mul_rn<T>(ri, F.inv_theta);
+    F.r[i] = ri;
+    F.d[i] = di;
+    F.x[i] = di;
+}
+
 // bc[coarse] = sum over restriction lists of rf[fine]  (coarse rows >= 1; row 0 = 0)
 template <class T>
 __global__ void k_restrict(const T* __restrict__ rf, T* __restrict__ bc, int ncx, int ncy, int ldf, int ldc,
                            const int* __restrict__ rpx, const int* __restrict__ rix, const T* __restrict__ rwx,
-                           const int* __restrict__ rpy, const int* __restrict__ riy, const T* __restrict__ rwy) {
+                           const int* __restrict__ rpy, const int* __restrict__ riy, const T* __restrict__ rwy,
+                           ChebFirst<T> F) {
     const int64_t N = (int64_t)ncx * ncy;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int cxi = (int)(i % ncx), cyi = (int)(i / ncx);
@@ -69,6 +91,7 @@ __global__ void k_restrict(const T* __restrict__ rf, T* __restrict__ bc, int ncx
             }
         }
         bc[(int64_t)cyi * ldc + cxi] = s;
+        cheb_first_pt(F, (int64_t)cyi * ldc + cxi, s);
     }
 }
 
@@ -102,7 +125,8 @@ __global__ void k_prolong_sem(const T* __restrict__ xc, T* __restrict__ xf, Layo
 
 // bc[vy, vx] = (P0^T rf)[vy, vx] over fine rows iy >= 1; coarse row 0 = 0.  One thread per vertex.
 template <class T>
-__global__ void k_restrict_sem(const T* __restrict__ rf, T* __restrict__ bc, Layout L, int ldc, GllW<T> w) {
+__global__ void k_restrict_sem(const T* __restrict__ rf, T* __restrict__ bc, Layout L, int ldc, GllW<T> w,
+                               ChebFirst<T> F) {
     const int vx = blockIdx.x * blockDim.x + threadIdx.x;
     const int vy = blockIdx.y;
     const int ncx = L.NelX + 1;
@@ -126,6 +150,7 @@ __global__ void k_restrict_sem(const T* __restrict__ rf, T* __restrict__ bc, Lay
         }
     }
     bc[(int64_t)vy * ldc + vx] = acc;
+    cheb_first_pt(F, (int64_t)vy * ldc + vx, acc);
 }
 
 // Chebyshev, first step.  with_x: r = Dinv (b - t) with t = A x ; else r = Dinv b, x = 0.
@@ -134,11 +159,11 @@ template <class T>
 __global__ void k_cheb_first(T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, const T* __restrict__ b,
                              const T* __restrict__ t, const T* __restrict__ Dinv, int64_t n, T inv_theta, int with_x) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T ri = with_x ? Dinv[i] * (b[i] - t[i]) : Dinv[i] * b[i];
-        const T di = ri * inv_theta;
+        const T ri = with_x ? mul_rn<T>(Dinv[i], sub_rn<T>(b[i], t[i])) : mul_rn<T>(Dinv[i], b[i]);
+        const T di = mul_rn<T>(ri, inv_theta);
         r[i] = ri;
         d[i] = di;
-        x[i] = with_x ? x[i] + di : di;
+        x[i] = with_x ? add_rn<T>(x[i], di) : di;
     }
 }
 // Chebyshev, later step: r -= Dinv t (t = A d) ; d = c1 d + c2 r ; x += d
@@ -146,11 +171,11 @@ template <class T>
 __global__ void k_cheb_step(T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, const T* __restrict__ t,
                             const T* __restrict__ Dinv, int64_t n, T c1, T c2) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T ri = r[i] - Dinv[i] * t[i];
-        const T di = c1 * d[i] + c2 * ri;
+        T ri = r[i], di = d[i], xi = x[i];
+        cheb_step_pt<T>(ri, di, xi, t[i], Dinv[i], c1, c2);
         r[i] = ri;
         d[i] = di;
-        x[i] += di;
+        x[i] = xi;
     }
 }
 // r = b - t
@@ -250,19 +275,42 @@ static void level_apply(Handle& h, int l, const T* x, T* y) {
         apply_K<T>(x, y, Sel<T>::args(h), T(1), 1, h.stream);
     } else {
         StencilLevel& L = m.lev[l - 1];
-        k_stencil<T><<<vb((int64_t)L.cx * L.cy), 256, 0, h.stream>>>(Sel<T>::A(L), x, y, L.cx, L.cy);
+        k_stencil<T><<<vb((int64_t)L.cx * L.cy), 256, 0, h.stream>>>(Sel<T>::A(L), x, y, L.cx, L.cy, OpEpi<T>());
         EQC_CHECK_LAUNCH();
         count_launch();
     }
+}
+
+// The operator of level l applied to x with the epilogue E (the level's residual or Chebyshev
+// step) in the same launch; false when level 0's selected apply kernel has no epilogue.
+static bool epi_apply(Handle& h, int l, const float* x, const OpEpi<float>& E) {
+    if (!h.fuse) return false;
+    if (l == 0) return apply_K_epi(x, args32(h), 1, E, h.stream);
+    StencilLevel& L = h.mg->lev[l - 1];
+    k_stencil<float><<<vb((int64_t)L.cx * L.cy), 256, 0, h.stream>>>(L.A32.p, x, nullptr, L.cx, L.cy, E);
+    EQC_CHECK_LAUNCH();
+    count_launch();
+    return true;
+}
+static bool epi_apply(Handle& h, int l, const double* x, const OpEpi<double>& E) {
+    if (l == 0 || !h.fuse) return false;   // the FP64 spectral-element apply has no epilogue
+    StencilLevel& L = h.mg->lev[l - 1];
+    k_stencil<double><<<vb((int64_t)L.cx * L.cy), 256, 0, h.stream>>>(L.A64.p, x, nullptr, L.cx, L.cy, E);
+    EQC_CHECK_LAUNCH();
+    count_launch();
+    return true;
 }
 
 static int64_t level_size(Handle& h, int l) {
     return l == 0 ? h.L.size() : (int64_t)h.mg->lev[l - 1].cx * h.mg->lev[l - 1].cy;
 }
 
-// Chebyshev smoothing of A_l x = b (deg steps), x = 0 initially when !with_x.
+// Chebyshev smoothing of A_l x = b (deg steps), x = 0 initially when !with_x.  first_done: the
+// first step (from x = 0) already ran inside the restriction that produced b.  Later steps run
+// fused into the operator (r, x updated in place, the direction alternating between the d and t
+// work vectors) when the level's operator kernel has the epilogue.
 template <class T>
-static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x) {
+static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x, bool first_done = false) {
     MGHier& m = *h.mg;
     MGWork& w = m.work[l];
     const int64_t n = level_size(h, l);
@@ -275,22 +323,48 @@ static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x) {
     T* r = Sel<T>::r(w);
     T* d = Sel<T>::d(w);
     T* t = Sel<T>::t(w);
-    if (with_x) level_apply<T>(h, l, x, t);
-    k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)(1.0 / theta), with_x ? 1 : 0);
-    count_launch();
-    const int deg = (l == 0) ? m.deg : m.deg_coarse;
-    for (int k = 1; k < deg; ++k) {
-        level_apply<T>(h, l, d, t);
-        const double rho_new = 1.0 / (2.0 * sigma - rho);
-        k_cheb_step<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, t, Dinv, n, (T)(rho_new * rho), (T)(2.0 * rho_new / delta));
+    if (!first_done) {
+        if (with_x) level_apply<T>(h, l, x, t);
+        k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)(1.0 / theta), with_x ? 1 : 0);
         count_launch();
+    }
+    const int deg = (l == 0) ? m.deg : m.deg_coarse;
+    T* dcur = d;
+    T* dnext = t;
+    for (int k = 1; k < deg; ++k) {
+        const double rho_new = 1.0 / (2.0 * sigma - rho);
+        const T c1 = (T)(rho_new * rho), c2 = (T)(2.0 * rho_new / delta);
+        OpEpi<T> E;
+        E.mode = 2;
+        E.r = r;
+        E.dinv = Dinv;
+        E.dold = dcur;
+        E.dnew = dnext;
+        E.x = x;
+        E.c1 = c1;
+        E.c2 = c2;
+        if (epi_apply(h, l, dcur, E)) {
+            std::swap(dcur, dnext);
+        } else {
+            level_apply<T>(h, l, dcur, t);
+            k_cheb_step<T><<<vb(n), 256, 0, h.stream>>>(x, r, dcur, t, Dinv, n, c1, c2);
+            count_launch();
+        }
         rho = rho_new;
     }
     EQC_CHECK_LAUNCH();
 }
 
+// 1 / theta of level l's Chebyshev interval (as chebyshev() computes it)
+static double cheb_inv_theta(const MGHier& m, int l) {
+    const double lmax = (l == 0) ? m.lmax0 : m.lev[l - 1].lmax;
+    const double lmin = lmax / m.lo_ratio;
+    return 1.0 / (0.5 * (lmax + lmin));
+}
+
+// first_done: the restriction that produced b already took level l's first smoothing step.
 template <class T>
-static void vcycle(Handle& h, int l, T* x, const T* b) {
+static void vcycle(Handle& h, int l, T* x, const T* b, bool first_done = false) {
     MGHier& m = *h.mg;
     const int L = (int)m.lev.size();
     if (l == m.cl_first && m.cl_size > 0) {   // the rest of the cycle in one cluster launch
@@ -309,27 +383,44 @@ static void vcycle(Handle& h, int l, T* x, const T* b) {
     }
     MGWork& w = m.work[l];
     const int64_t n = level_size(h, l);
-    chebyshev<T>(h, l, x, b, false);
-    // residual
+    chebyshev<T>(h, l, x, b, false, first_done);
+    // residual r = b - A x, fused into the operator where it has the epilogue
     T* t = Sel<T>::t(w);
     T* r = Sel<T>::r(w);
-    level_apply<T>(h, l, x, t);
-    k_sub<T><<<vb(n), 256, 0, h.stream>>>(b, t, r, n);
-    count_launch();
+    OpEpi<T> E;
+    E.mode = 1;
+    E.b = b;
+    E.r = r;
+    if (!epi_apply(h, l, x, E)) {
+        level_apply<T>(h, l, x, t);
+        k_sub<T><<<vb(n), 256, 0, h.stream>>>(b, t, r, n);
+        count_launch();
+    }
     DevTransfer& tr = m.T[l];
     MGWork& wc = m.work[l + 1];
     T* bc = Sel<T>::b(wc);
     T* xc = Sel<T>::x(wc);
     const GllW<T> gw = gll_weights<T>(m);
+    // the coarse level's first smoothing step rides on the restriction (not into the dense level
+    // or a cluster-resident cycle)
+    ChebFirst<T> F;
+    const bool fuse = h.fuse && l + 1 < L && !(l + 1 == m.cl_first && m.cl_size > 0);
+    if (fuse) {
+        F.dinv = Sel<T>::Di(m.lev[l]);
+        F.x = xc;
+        F.r = Sel<T>::r(wc);
+        F.d = Sel<T>::d(wc);
+        F.inv_theta = (T)cheb_inv_theta(m, l + 1);
+    }
     if (l == 0) {
-        k_restrict_sem<T><<<dim3((tr.ncx + 127) / 128, tr.ncy), 128, 0, h.stream>>>(r, bc, h.L, tr.ldc, gw);
+        k_restrict_sem<T><<<dim3((tr.ncx + 127) / 128, tr.ncy), 128, 0, h.stream>>>(r, bc, h.L, tr.ldc, gw, F);
     } else {
         k_restrict<T><<<vb((int64_t)tr.ncx * tr.ncy), 256, 0, h.stream>>>(r, bc, tr.ncx, tr.ncy, tr.ldf, tr.ldc,
                                                                            tr.rpx.p, tr.rix.p, Sel<T>::rwx(tr), tr.rpy.p,
-                                                                           tr.riy.p, Sel<T>::rwy(tr));
+                                                                           tr.riy.p, Sel<T>::rwy(tr), F);
     }
     count_launch();
-    vcycle<T>(h, l + 1, xc, bc);
+    vcycle<T>(h, l + 1, xc, bc, fuse);
     if (l == 0) {
         k_prolong_sem<T><<<dim3((h.L.NelX + 127) / 128, h.L.ny - 1), 128, 0, h.stream>>>(xc, x, h.L, tr.ldc, gw);
     } else {

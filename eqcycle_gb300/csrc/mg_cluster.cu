@@ -13,6 +13,7 @@
 // double-buffered (d <-> t), so one phase computes t = A d_old, r -= Dinv t,
 // d_new = c1 d_old + c2 r and x += d_new.
 #include "mg.h"
+#include "epi.cuh"
 #include "reduce.cuh"
 
 namespace eqc {
@@ -75,11 +76,11 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_cycle(ClusterArgs<T> P) {
             for (int64_t i = tid; i < N; i += nthr) {
                 const int ix = (int)(i % cx), iy = (int)(i / cx);
                 const T ti = iy >= 1 ? stencil_at(L.A, d, ix, iy, cx, cy, N) : T(0);
-                const T ri = ldc(r + i) - L.Dinv[i] * ti;
-                const T di = L.c1[k] * ldc(d + i) + L.c2[k] * ri;
+                T ri = ldc(r + i), di = ldc(d + i), xi = ldc(x + i);
+                cheb_step_pt<T>(ri, di, xi, ti, L.Dinv[i], L.c1[k], L.c2[k]);
                 r[i] = ri;
                 dn[i] = di;
-                x[i] = ldc(x + i) + di;
+                x[i] = xi;
             }
             T* tmp = d; d = dn; dn = tmp;
             cluster_sync_all();
@@ -174,11 +175,11 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_cycle(ClusterArgs<T> P) {
                 const int ix = (int)(i % cx), iy = (int)(i / cx);
                 const T ti = iy >= 1 ? stencil_at(L.A, d, ix, iy, cx, cy, N) : T(0);
                 const T dold = ldc(d + i);
-                const T ri = ldc(r + i) - L.Dinv[i] * ti;
-                const T di = L.c1[k] * dold + L.c2[k] * ri;
+                T ri = ldc(r + i), di = dold, xi = (k == 1) ? add_rn<T>(ldc(x + i), dold) : ldc(x + i);
+                cheb_step_pt<T>(ri, di, xi, ti, L.Dinv[i], L.c1[k], L.c2[k]);
                 r[i] = ri;
                 dn[i] = di;
-                x[i] = (k == 1) ? ldc(x + i) + dold + di : ldc(x + i) + di;
+                x[i] = xi;
             }
             T* tmp = d; d = dn; dn = tmp;
             cluster_sync_all();

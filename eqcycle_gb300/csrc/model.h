@@ -1,6 +1,7 @@
 // The handle: one fault model resident on one GPU.
 #pragma once
 #include "common.h"
+#include "epi.cuh"
 #include <memory>
 
 namespace eqc {
@@ -91,7 +92,10 @@ struct Handle {
     double damage_factor = 1.0;
     int64_t damage_count = 0;
     int64_t gen = 0;
-    double setup_ms[5] = {0, 0, 0, 0, 0};   // eqc_create phases: numbering, elements, nodes, other, hierarchy
+    double setup_ms[5] = {0, 0, 0, 0, 0};
+    // V-cycle pointwise work fused into the operator kernels (EQC_NO_FUSE set at creation: the
+    // separate kernels, for comparisons)
+    bool fuse = true;   // eqc_create phases: numbering, elements, nodes, other, hierarchy
     // Stream that work is enqueued on: the handle's own stream, or, while a conditional
     // body of a step graph is being captured, that body's capture stream.
     cudaStream_t stream = nullptr;
@@ -174,6 +178,9 @@ inline ApplyArgs<float> args32(Handle& h) {
     return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant};
 }
 void tma_init(Handle& h);
+// FP32 apply y = K x (mode 0/1 as apply_K) whose owned nodes are finished by the epilogue E
+// (residual or Chebyshev step) instead of stored; false when the selected kernel has none.
+bool apply_K_epi(const float* x, const ApplyArgs<float>& A, int mode, const OpEpi<float>& E, cudaStream_t s);
 
 // blas.cu
 void dot64(Handle& h, const double* x, const double* y, int64_t n, double* out_dev);

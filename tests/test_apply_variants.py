@@ -51,3 +51,29 @@ def test_fp32_apply_kernels_agree(eqclib, name):
     y32, y64 = out[8][:, :nx].astype(np.float64), out["f64"][:, :nx]
     assert np.max(np.abs(y32 - y64)) <= 1e-5 * np.max(np.abs(y64))
     assert not np.any(out[8][:, nx:])   # row padding untouched
+
+
+@pytest.mark.parametrize("variant", [0, 8])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_fused_vcycle_equals_separate_kernels(eqclib, monkeypatch, variant, precision):
+    """The V-cycle's residuals, Chebyshev steps and first coarse smoothing steps fused into the
+    operator and restriction kernels give the same bits as the separate vector kernels
+    (EQC_NO_FUSE), through quasi-static steps of the damage-zone model."""
+    from eqcycle_gb300 import EQC_FP64, EQC_MIXED, EQC_PC_AMG
+    cfg = preset("dz40")
+    P = set_parameters(cfg)
+    prec = EQC_MIXED if precision == "mixed" else EQC_FP64
+    out = []
+    for no_fuse in (False, True):
+        if no_fuse:
+            monkeypatch.setenv("EQC_NO_FUSE", "1")
+        else:
+            monkeypatch.delenv("EQC_NO_FUSE", raising=False)
+        with Solver(P, precision=prec, precond=EQC_PC_AMG, guess=2, apply_variant=variant, mg_degree=4,
+                    mg_degree_coarse=3) as s:
+            s.init(cfg.V_init)
+            st = s.run(8)
+            out.append((st["cg_iters"], {k: s.state(k) for k in ("d", "psi", "tau")}))
+    assert out[0][0] == out[1][0]
+    for k in out[0][1]:
+        assert np.array_equal(out[0][1][k], out[1][1][k]), k
