@@ -170,6 +170,14 @@ def steady_dt(solver, P):
     return solver.dtevol(1e30, P.float_.dt0, Vf, 1)
 
 
+L2_BYTES = 129 * 2 ** 20   # GB300's L2
+
+
+def stream_copies(nbytes: int) -> int:
+    """Working-set replicas whose total is at least twice L2 (each launch then reads from HBM)."""
+    return int(min(64, max(2, -(-2 * L2_BYTES // max(nbytes, 1)))))
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -287,8 +295,10 @@ def bench_ours(args):
     e2e_value = _allreduce(dist, e2e_years, _sum_op()) / (e2e_s_max / 3600.0)
     # ---- roofline of the dominant kernel (FP32 stiffness apply, L2 flushed between launches)
     peak, peak_kind = measured_peaks()
-    ms32 = s.time_apply(1, 50, True)
+    ms32_cold = s.time_apply(1, 50, True)
     bytes32 = 4 * (2 * nglob + 25 * Nel)
+    nc32 = stream_copies(bytes32)
+    ms32 = s.time_apply_stream(1, 12 * nc32, nc32)
     ms64 = s.time_apply(0, 20, True)
     bytes64 = 8 * (2 * nglob + 25 * Nel)
     # DRAM bytes per launch of the kernel the autotuner chose, from one ncu capture
@@ -341,7 +351,7 @@ def bench_ours(args):
                                f"start; mixed-precision multigrid-PCG (tol 1e-8), extrapolated initial guess, "
                                f"autotuned smoother",
                    "nodes": nglob, "fault_nodes": Nf, "parallelism": f"replicas x{ws}",
-                   "l2": "stiffness-apply roofline timed with an L2 flush between launches"},
+                   "l2": "stiffness-apply roofline: launches rotate over working-set replicas larger than L2"},
         "qs_step_ms": 1e3 * dev_s / max(st["qs_steps"], 1), "cg_iters_per_solve": st["cg_iters"] / max(st["qs_solves"], 1),
         "sim_years_in_window": sim_years,
         "plain_fp64": leg(st64, sy64),
@@ -354,7 +364,11 @@ def bench_ours(args):
                      "frac": bytes32 / (ms32 * 1e-3) / 1e9 / peak, "traffic": traffic,
                      "kernel": f"{kname} (FP32 stiffness apply, one element per lane; chosen by the autotuner)",
                      "peak_kind": peak_kind,
-                     "launch_us": ms32 * 1e3, "algorithmic_bytes": bytes32},
+                     "launch_us": ms32 * 1e3, "algorithmic_bytes": bytes32,
+                     "timing": f"{12 * nc32} back-to-back launches rotating over {nc32} replicas of the working set "
+                               f"({nc32 * bytes32 / 2 ** 20:.0f} MiB > L2), CUDA events around the batch",
+                     "single_launch_l2_flushed_us": ms32_cold * 1e3,
+                     "single_launch_frac": bytes32 / (ms32_cold * 1e-3) / 1e9 / peak},
         "fp64_apply": {"launch_us": ms64 * 1e3, "algorithmic_bytes": bytes64,
                        "achieved_gbs": bytes64 / (ms64 * 1e-3) / 1e9},
         "gpu_launches": launches,
@@ -436,8 +450,12 @@ def bench_kernel(args):
                 continue
             ms = s.time_apply(dt, args.nrep, True)
             B = es * (2 * nglob + 25 * Nel)
+            nc = stream_copies(B)
+            mss = s.time_apply_stream(dt, max(args.nrep, 4 * nc), nc)
             out[name] = {"launch_us": ms * 1e3, "algorithmic_bytes": B, "achieved_gbs": B / ms / 1e6,
-                         "frac": B / ms / 1e6 / peak}
+                         "frac": B / ms / 1e6 / peak,
+                         "stream": {"launch_us": mss * 1e3, "copies": nc, "achieved_gbs": B / mss / 1e6,
+                                    "frac": B / mss / 1e6 / peak}}
     print(json.dumps(out), flush=True)
 
 

@@ -72,7 +72,7 @@ _lib: Optional[C.CDLL] = None
 EXPORTS = ["eqc_default_options", "eqc_create", "eqc_destroy", "eqc_last_error", "eqc_apply_K", "eqc_qs_solve",
            "eqc_slrFunc", "eqc_FBC", "eqc_dtevol", "eqc_dtevol_noalloc", "eqc_init", "eqc_run", "eqc_get_state", "eqc_set_state",
            "eqc_get_scalar", "eqc_set_scalar", "eqc_result_size", "eqc_get_result", "eqc_layout", "eqc_apply_K_device",
-           "eqc_time_apply", "eqc_launch_count", "eqc_sync", "eqc_set_damage", "eqc_damage_evolve", "eqc_create_structured", "eqc_guess_shape", "eqc_guess_init",
+           "eqc_time_apply", "eqc_time_apply_stream", "eqc_launch_count", "eqc_sync", "eqc_set_damage", "eqc_damage_evolve", "eqc_create_structured", "eqc_guess_shape", "eqc_guess_init",
            "eqc_guess_get_params", "eqc_guess_set_params", "eqc_guess_log", "eqc_guess_pairs", "eqc_guess_train",
            "eqc_guess_eval", "eqc_guess_grad", "eqc_autotune", "eqc_ensemble_create", "eqc_ensemble_run",
            "eqc_ensemble_destroy", "eqc_ensemble_last_error"]
@@ -111,6 +111,7 @@ def lib() -> C.CDLL:
     L.eqc_layout.argtypes = [P, _ip, _ip, _ip]
     L.eqc_apply_K_device.argtypes = [P, P, P, I32]
     L.eqc_time_apply.argtypes = [P, I32, I32, I32, _dp]
+    L.eqc_time_apply_stream.argtypes = [P, I32, I32, I32, _dp]
     L.eqc_launch_count.restype = I64
     L.eqc_launch_count.argtypes = [P]
     L.eqc_sync.argtypes = [P]

@@ -660,10 +660,7 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
         mbar_fence_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        issue(0);
-        if (nt > 1) issue(1);
-    }
+    if (threadIdx.x == 0) issue(0);   // the first tile alone: it reaches every CTA before any second one
     const int ex = ex0 - 1 + lane;
     for (int k = 0; k < nt; ++k) {
         const int st = k & 1;
@@ -671,15 +668,17 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
         bool done = false;
         for (int it = 0; it < MBAR_SPIN_LIMIT && !done; ++it) done = mbar_try_wait(&bar[st], parity);
         if (__syncthreads_or(!done)) {
-            // give up: flag it, wait (bounded) for the copies still in flight (tiles k, k + 1), leave
+            // give up: flag it, wait (bounded) for the copies still in flight (tile 0, or tiles
+            // k and k + 1), leave
             if (threadIdx.x == 0) {
                 if (A.err) atomicExch(A.err, 1);
-                for (int j = k; j < nt && j < k + 2; ++j)
+                for (int j = k; j < nt && j < (k == 0 ? 1 : k + 2); ++j)
                     for (int it = 0; it < MBAR_SPIN_LIMIT; ++it)
                         if (mbar_try_wait(&bar[j & 1], (uint32_t)((j >> 1) & 1))) break;
             }
             return;
         }
+        if (k == 0 && nt > 1 && threadIdx.x == 0) issue(1);   // overlaps the first tile's compute
         const int ey = r0 - 1 + WK_ROWS * k + w;
         if (ey >= r_end) {   // past the walk (warp-uniform): no row to compute, only the barrier
             __syncthreads();
@@ -847,21 +846,24 @@ static const CUtensorMap* tma_umap_walk(TmaCache& c, const float* x, const Layou
     return &(c.u32walk[x] = tm);
 }
 
-// Encodes the element-data maps; leaves the cache disabled (plain loads) if TMA is unavailable.
-void tma_init(Handle& h) {
-    TmaCache& c = h.tma;
+// Encodes the element-data maps of the padded W copies W32p / W64p; leaves the cache disabled
+// (plain loads) if TMA is unavailable.
+void tma_init_for(TmaCache& c, const Layout& L, const float* W32p, const double* W64p) {
     c.ok = false;
     c.walk_ok = false;
+    c.u32.clear();
+    c.u64.clear();
+    c.u32walk.clear();
     if (getenv("EQC_NO_TMA")) return;
-    const Layout& L = h.L;
     const int EX = LTEX + 1, EY = LTEY + 1;
-    bool ok = encode_2d(&c.w32, false, h.W32p.p, (uint64_t)L.NelX * WPad<float>::v, (uint64_t)L.NelY,
+    bool ok = encode_2d(&c.w32, false, W32p, (uint64_t)L.NelX * WPad<float>::v, (uint64_t)L.NelY,
                         (uint64_t)L.NelX * WPad<float>::v * sizeof(float), EX * WPad<float>::v, EY);
-    ok = ok && encode_2d(&c.w64, true, h.W64p.p, (uint64_t)L.NelX * WPad<double>::v, (uint64_t)L.NelY,
+    ok = ok && encode_2d(&c.w64, true, W64p, (uint64_t)L.NelX * WPad<double>::v, (uint64_t)L.NelY,
                          (uint64_t)L.NelX * WPad<double>::v * sizeof(double), EX * WPad<double>::v, EY);
     c.ok = ok;
-    c.walk_ok = ok && encode_w_walk(&c.w32walk, h.W32p.p, L.NelX, L.NelY);
+    c.walk_ok = ok && encode_w_walk(&c.w32walk, W32p, L.NelX, L.NelY);
 }
+void tma_init(Handle& h) { tma_init_for(h.tma, h.L, h.W32p.p, h.W64p.p); }
 
 // CTAs of the pipelined apply: as many as fit on every SM at once.
 static int g_pipe_blocks[2] = {0, 0};

@@ -178,6 +178,7 @@ inline ApplyArgs<float> args32(Handle& h) {
     return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant};
 }
 void tma_init(Handle& h);
+void tma_init_for(TmaCache& c, const Layout& L, const float* W32p, const double* W64p);
 // FP32 apply y = K x (mode 0/1 as apply_K) whose owned nodes are finished by the epilogue E
 // (residual or Chebyshev step) instead of stored; false when the selected kernel has none.
 bool apply_K_epi(const float* x, const ApplyArgs<float>& A, int mode, const OpEpi<float>& E, cudaStream_t s);

@@ -290,6 +290,12 @@ class Solver:
         self._chk(L.lib().eqc_time_apply(self.h, dtype, nrep, int(flush_l2), C.byref(ms)))
         return ms.value
 
+    def time_apply_stream(self, dtype: int = 1, nrep: int = 60, ncopies: int = 6) -> float:
+        """Mean duration (ms) of back-to-back applies rotating over ncopies working-set replicas."""
+        ms = C.c_double(0)
+        self._chk(L.lib().eqc_time_apply_stream(self.h, dtype, nrep, ncopies, C.byref(ms)))
+        return ms.value
+
     def launches(self) -> int:
         return int(L.lib().eqc_launch_count(self.h))
 

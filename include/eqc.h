@@ -311,6 +311,12 @@ eqc_status eqc_apply_K_device(eqc_handle* h, const void* x, void* y, int32_t dty
  * launch duration. */
 eqc_status eqc_time_apply(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t flush_l2, double* ms);
 
+/* Time nrep back-to-back launches of the stiffness apply rotating over ncopies replicas of its
+ * whole working set (x, y, W), so that with replicas larger than L2 together every launch
+ * streams its data from HBM; *ms gets the mean launch duration (CUDA events around the
+ * batch, on the handle's stream). */
+eqc_status eqc_time_apply_stream(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t ncopies, double* ms);
+
 /* Solver autotuner (no counterpart in the reference): times `reps` graph-replayed trial
  * solves of the next quasi-static solve from the current state for a set of Chebyshev
  * degrees (spectral-element level x vertex levels) and keeps the fastest; in mixed precision
