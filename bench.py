@@ -415,6 +415,25 @@ def bench_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_profile_steps(args):
+    """The headline method on the workload, host-driven (every kernel a separate launch, for an
+    ncu launch list), with its solver settings given on the command line instead of autotuned
+    (an autotuner timed under a profiler chooses differently): W warm-up steps, then K steps;
+    prints how many kernels the K steps launched (the tail of the launch list)."""
+    from eqcycle_gb300 import EQC_GUESS_EXTRAPOLATE, EQC_MIXED, Solver, preset, set_parameters
+    P = set_parameters(preset(args.workload))
+    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, guess=EQC_GUESS_EXTRAPOLATE, use_graphs=0,
+               apply_variant=args.apply_variant, mg_degree=args.mg_degree, mg_degree_coarse=args.mg_degree_coarse,
+               reliable_delta=args.reliable_delta)
+    s.init(P.cfg.V_init)
+    s.set_scalar("dt", steady_dt(s, P))
+    s.run(args.warmup)
+    l0 = s.launches()
+    st = s.run(args.steps)
+    print(json.dumps({"workload": args.workload, "launches_in_steps": s.launches() - l0, "steps": st}), flush=True)
+    s.close()
+
+
 def bench_setup(args):
     """Model setup time on the workload mesh: the host setup (set_parameters over the whole mesh,
     then eqc_create uploading iglob/W/M) against the setup on the device (structured_parameters
@@ -623,6 +642,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true", help="time the stiffness apply alone")
     ap.add_argument("--setup", action="store_true", help="time the model setup, host against device")
+    ap.add_argument("--profile-steps", action="store_true",
+                    help="host-driven headline steps with the solver settings below, for an ncu launch list")
+    ap.add_argument("--mg-degree", type=int, default=0, help="with --profile-steps: SEM-level Chebyshev degree")
+    ap.add_argument("--mg-degree-coarse", type=int, default=0, help="with --profile-steps: vertex-level degree")
+    ap.add_argument("--reliable-delta", type=float, default=0.0, help="with --profile-steps: update factor")
     ap.add_argument("--dtype", default="both", choices=["both", "f32", "f64"])
     ap.add_argument("--nrep", type=int, default=20)
     ap.add_argument("--learned", action="store_true", help="learned initial guess: train and evaluate")
@@ -639,7 +663,7 @@ def main():
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--apply-variant", type=int, default=0,
                     help="stiffness apply kernel: 0 default, 1 one tile per CTA (TMA), 2 plain tile loads, "
-                         "3 persistent TMA pipeline")
+                         "3 persistent TMA pipeline, 4-7 element per lane with 4/8/12/6 rows per CTA, 8 TMA walk")
     args = ap.parse_args()
     if args.workload is None and not args.cycle:
         args.workload = "dz480"
@@ -647,6 +671,8 @@ def main():
         bench_kernel(args)
     elif args.setup:
         bench_setup(args)
+    elif args.profile_steps:
+        bench_profile_steps(args)
     elif args.learned:
         bench_learned(args)
     elif args.ensemble:
