@@ -550,12 +550,12 @@ def bench_ensemble(args):
     parameters) advanced by one CUDA-graph launch per step, mixed precision with the extrapolated
     guess; compared with the same members stepped one after another with their own graphs."""
     from eqcycle_gb300 import (EQC_GUESS_EXTRAPOLATE, EQC_MIXED, Ensemble, Solver, ensemble_members,
-                               set_parameters)
+                               structured_parameters)
     t0 = time.time()
     cfgs = ensemble_members(args.members)
     solvers, nodes = [], 0
     for c in cfgs:
-        P = set_parameters(c)
+        P = structured_parameters(c)   # element and node data built on the device
         s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, guess=EQC_GUESS_EXTRAPOLATE)
         s.init(c.V_init)
         s.set_scalar("dt", steady_dt(s, P))
