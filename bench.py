@@ -422,11 +422,14 @@ def bench_profile_steps(args):
     prints how many kernels the K steps launched (the tail of the launch list)."""
     from eqcycle_gb300 import EQC_GUESS_EXTRAPOLATE, EQC_MIXED, Solver, preset, set_parameters
     P = set_parameters(preset(args.workload))
-    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, guess=EQC_GUESS_EXTRAPOLATE, use_graphs=0,
+    s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, guess=EQC_GUESS_EXTRAPOLATE, use_graphs=1 if args.graphs else 0,
                apply_variant=args.apply_variant, mg_degree=args.mg_degree, mg_degree_coarse=args.mg_degree_coarse,
                reliable_delta=args.reliable_delta)
-    s.init(P.cfg.V_init)
-    s.set_scalar("dt", steady_dt(s, P))
+    if args.dynamic:   # Newmark steps: the fault sliding at 5 cm/s, above the regime threshold
+        s.init(5e-2)
+    else:
+        s.init(P.cfg.V_init)
+        s.set_scalar("dt", steady_dt(s, P))
     s.run(args.warmup)
     l0 = s.launches()
     st = s.run(args.steps)
@@ -644,6 +647,8 @@ def main():
     ap.add_argument("--setup", action="store_true", help="time the model setup, host against device")
     ap.add_argument("--profile-steps", action="store_true",
                     help="host-driven headline steps with the solver settings below, for an ncu launch list")
+    ap.add_argument("--dynamic", action="store_true", help="with --profile-steps: dynamic (Newmark) steps")
+    ap.add_argument("--graphs", action="store_true", help="with --profile-steps: graph-replayed (batched) steps")
     ap.add_argument("--mg-degree", type=int, default=0, help="with --profile-steps: SEM-level Chebyshev degree")
     ap.add_argument("--mg-degree-coarse", type=int, default=0, help="with --profile-steps: vertex-level degree")
     ap.add_argument("--reliable-delta", type=float, default=0.0, help="with --profile-steps: update factor")

@@ -77,3 +77,4 @@ def test_fused_vcycle_equals_separate_kernels(eqclib, monkeypatch, variant, prec
     assert out[0][0] == out[1][0]
     for k in out[0][1]:
         assert np.array_equal(out[0][1][k], out[1][1][k]), k
+
