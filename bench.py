@@ -262,7 +262,7 @@ def bench_ours(args):
     if args.warmup:
         s.run(args.warmup)
     t_tune = time.time()
-    tuned = s.autotune(reps=2)   # after the warm-up: trial solves of a representative step
+    tuned = s.autotune(reps=3)   # after the warm-up: trial solves of a representative step
     tuned["wall_s"] = time.time() - t_tune
     start = {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}
     t_start, dt_start, iso_start = s.scalar("t"), s.scalar("dt"), s.scalar("isolver")
