@@ -300,6 +300,7 @@ def bench_ours(args):
     nc32 = stream_copies(bytes32)
     ms32 = s.time_apply_stream(1, 12 * nc32, nc32)
     ms64 = s.time_apply(0, 20, True)
+    msdf = s.time_apply(2, 20, True)
     bytes64 = 8 * (2 * nglob + 25 * Nel)
     # DRAM bytes per launch of the kernel the autotuner chose, from one ncu capture
     kname = APPLY_KERNELS.get(tuned.get("apply_variant", 0), "k_apply_rows<6,3>")
@@ -370,7 +371,8 @@ def bench_ours(args):
                      "single_launch_l2_flushed_us": ms32_cold * 1e3,
                      "single_launch_frac": bytes32 / (ms32_cold * 1e-3) / 1e9 / peak},
         "fp64_apply": {"launch_us": ms64 * 1e3, "algorithmic_bytes": bytes64,
-                       "achieved_gbs": bytes64 / (ms64 * 1e-3) / 1e9},
+                       "achieved_gbs": bytes64 / (ms64 * 1e-3) / 1e9,
+                       "double_float_launch_us": msdf * 1e3},
         "gpu_launches": launches,
     }
     line["speedup_vs_plain_fp64"] = value / line["plain_fp64"]["value"] if line["plain_fp64"]["value"] else None

@@ -64,14 +64,16 @@ static void load_element_data(Handle& h, const double* W) {
         h.diag64.alloc(L.size());
         h.diag32.alloc(L.size());
     }
+    if (!h.W32lo.p) h.W32lo.alloc((size_t)WPad<float>::v * Nel);
     std::vector<float> w32(nW);
     for (size_t k = 0; k < nW; ++k) w32[k] = (float)W[k];
     const int p32 = WPad<float>::v, p64 = WPad<double>::v;
-    std::vector<float> a((size_t)p32 * Nel, 0.f);
+    std::vector<float> a((size_t)p32 * Nel, 0.f), alo((size_t)p32 * Nel, 0.f);
     std::vector<double> b((size_t)p64 * Nel, 0.0);
     for (int64_t e = 0; e < Nel; ++e)
         for (int q = 0; q < 25; ++q) {
             a[(size_t)p32 * e + q] = w32[(size_t)25 * e + q];
+            alo[(size_t)p32 * e + q] = (float)(W[(size_t)25 * e + q] - (double)w32[(size_t)25 * e + q]);
             b[(size_t)p64 * e + q] = W[(size_t)25 * e + q];
         }
     std::vector<double> dg = diag_K(h, W);
@@ -81,6 +83,7 @@ static void load_element_data(Handle& h, const double* W) {
     h.W64.upload(W, nW, s);
     h.W32.upload(w32.data(), nW, s);
     h.W32p.upload(a.data(), a.size(), s);
+    h.W32lo.upload(alo.data(), alo.size(), s);
     h.W64p.upload(b.data(), b.size(), s);
     h.diag64.upload(dg.data(), dg.size(), s);
     h.diag32.upload(dg32.data(), dg32.size(), s);
@@ -159,6 +162,14 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     h.yr2sec = (double)m.yr2sec;
     std::memcpy(h.H, m.H, sizeof(h.H));
     set_H(h.H, s);
+    set_H_df(h.H, s);
+    {   // the double-float apply uses the even-odd form: H must be centro-antisymmetric
+        double hmax = 0.0, asym = 0.0;
+        for (int k = 0; k < 25; ++k) hmax = std::max(hmax, std::fabs(h.H[k]));
+        for (int i = 0; i < 5; ++i)
+            for (int j = 0; j < 5; ++j) asym = std::max(asym, std::fabs(h.H[i + 5 * j] + h.H[(4 - i) + 5 * (4 - j)]));
+        h.df_ok = asym <= 1e-12 * hmax && std::getenv("EQC_NO_DF") == nullptr;
+    }
     using clk = std::chrono::steady_clock;
     auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
     auto t0 = clk::now();
@@ -663,11 +674,13 @@ eqc_status eqc_damage_evolve(eqc_handle* H) {
 }
 
 eqc_status eqc_apply_K_device(eqc_handle* H, const void* x, void* y, int32_t dtype) {
-    if (!H || !x || !y || (dtype != 0 && dtype != 1)) return EQC_E_ARG;
+    if (!H || !x || !y || dtype < 0 || dtype > 2) return EQC_E_ARG;
     return guarded(H, [&] {
         Handle& h = H->h;
         if (dtype == 0) apply_K<double>((const double*)x, (double*)y, args64(h), 1.0, 0, h.stream);
-        else apply_K<float>((const float*)x, (float*)y, args32(h), 1.0f, 0, h.stream);
+        else if (dtype == 1) apply_K<float>((const float*)x, (float*)y, args32(h), 1.0f, 0, h.stream);
+        else if (!apply_K_df(h, (const double*)x, (double*)y, 1.0, 0, h.stream))
+            throw Error(EQC_E_STATE, "double-float apply unavailable (EQC_NO_DF, or H not centro-antisymmetric)");
     });
 }
 

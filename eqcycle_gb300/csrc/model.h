@@ -117,6 +117,8 @@ struct Handle {
     // element data
     DBuf<double> W64, W64p;
     DBuf<float> W32, W32p;
+    DBuf<float> W32lo;   // W - W32p rounded to FP32 (padded like W32p): W as double-float
+    bool df_ok = false;  // the double-float FP64-class apply is usable (EQC_NO_DF unset, H symmetric)
     TmaCache tma;
     double H[25];
     // node arrays [L.size()]
@@ -178,6 +180,9 @@ inline ApplyArgs<float> args32(Handle& h) {
     return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant};
 }
 void tma_init(Handle& h);
+void set_H_df(const double* H, cudaStream_t s);
+// y = sign K x (FP64 vectors, mode 0/1) in double-float arithmetic; false when unavailable.
+bool apply_K_df(Handle& h, const double* x, double* y, double sign, int mode, cudaStream_t s);
 void tma_init_for(TmaCache& c, const Layout& L, const float* W32p, const double* W64p);
 // FP32 apply y = K x (mode 0/1 as apply_K) whose owned nodes are finished by the epilogue E
 // (residual or Chebyshev step) instead of stored; false when the selected kernel has none.

@@ -42,7 +42,7 @@ __device__ __forceinline__ void material(const SetupArgs& a, int ex, int ey, int
 
 // One thread per element: W (FP64, FP32 and the copies padded for TMA element tiles).
 __global__ void k_setup_W(SetupArgs a, double* __restrict__ W64, float* __restrict__ W32, double* __restrict__ W64p,
-                          float* __restrict__ W32p) {
+                          float* __restrict__ W32p, float* __restrict__ W32lo) {
     const int64_t Nel = (int64_t)a.L.NelX * a.L.NelY;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nel; e += (int64_t)gridDim.x * blockDim.x) {
         const int ex = (int)(e % a.L.NelX), ey = (int)(e / a.L.NelX);
@@ -55,9 +55,13 @@ __global__ void k_setup_W(SetupArgs a, double* __restrict__ W64, float* __restri
                 W32[25 * e + i + 5 * j] = (float)w;
                 W64p[(int64_t)WPad<double>::v * e + i + 5 * j] = w;
                 W32p[(int64_t)WPad<float>::v * e + i + 5 * j] = (float)w;
+                W32lo[(int64_t)WPad<float>::v * e + i + 5 * j] = (float)(w - (double)(float)w);
             }
         for (int q = 25; q < WPad<double>::v; ++q) W64p[(int64_t)WPad<double>::v * e + q] = 0.0;
-        for (int q = 25; q < WPad<float>::v; ++q) W32p[(int64_t)WPad<float>::v * e + q] = 0.f;
+        for (int q = 25; q < WPad<float>::v; ++q) {
+            W32p[(int64_t)WPad<float>::v * e + q] = 0.f;
+            W32lo[(int64_t)WPad<float>::v * e + q] = 0.f;
+        }
     }
 }
 
@@ -142,10 +146,11 @@ void setup_element_data_device(Handle& h, const eqc_material& mat) {
     h.W32.alloc((size_t)25 * Nel);
     h.W64p.alloc((size_t)WPad<double>::v * Nel);
     h.W32p.alloc((size_t)WPad<float>::v * Nel);
+    h.W32lo.alloc((size_t)WPad<float>::v * Nel);
     h.diag64.alloc(h.L.size());
     h.diag32.alloc(h.L.size());
     const int blocks = (int)std::min<int64_t>((Nel + 255) / 256, 4096);
-    k_setup_W<<<blocks, 256, 0, h.stream>>>(a, h.W64.p, h.W32.p, h.W64p.p, h.W32p.p);
+    k_setup_W<<<blocks, 256, 0, h.stream>>>(a, h.W64.p, h.W32.p, h.W64p.p, h.W32p.p, h.W32lo.p);
     EQC_CHECK_LAUNCH();
     count_launch();
 }

@@ -432,6 +432,8 @@ static void update_mixed(Handle& h) {
     const int64_t ld = L.ld, n = L.size() - ld;
     CGState* S = h.cg.p;
     k_fold<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.d.p + ld, h.x32.p + ld, n, S);
+    // FP64, not the double-float apply: late in a cycle |K||x| / |b| grows until its ~1e-14
+    // relative error floors the true residual near 1e-5 of |b| (measured), above the tolerance
     apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);
     k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p, h.red_count.p,
                                                          S);

@@ -21,12 +21,12 @@ __global__ void k_flush(const float4* __restrict__ buf, int64_t n4, float* sink)
 using namespace eqc;
 
 extern "C" eqc_status eqc_time_apply(eqc_handle* H, int32_t dtype, int32_t nrep, int32_t flush_l2, double* ms) {
-    if (!H || !ms || nrep < 1 || (dtype != 0 && dtype != 1)) return EQC_E_ARG;
+    if (!H || !ms || nrep < 1 || dtype < 0 || dtype > 2) return EQC_E_ARG;
     Handle& h = H->h;
     try {
         cudaStream_t s = h.stream;
         const int64_t N = h.L.size();
-        const size_t es = dtype == 0 ? sizeof(double) : sizeof(float);
+        const size_t es = dtype == 1 ? sizeof(float) : sizeof(double);
         void *x = nullptr, *y = nullptr;
         float* fl = nullptr;
         const int64_t nfl = (int64_t)(512ull << 20) / 4;  // 512 MB > L2
@@ -46,7 +46,9 @@ extern "C" eqc_status eqc_time_apply(eqc_handle* H, int32_t dtype, int32_t nrep,
             }
             EQC_CUDA(cudaEventRecord(e0, s));
             if (dtype == 0) apply_K<double>((const double*)x, (double*)y, args64(h), 1.0, 0, s);
-            else apply_K<float>((const float*)x, (float*)y, args32(h), 1.0f, 0, s);
+            else if (dtype == 1) apply_K<float>((const float*)x, (float*)y, args32(h), 1.0f, 0, s);
+            else if (!apply_K_df(h, (const double*)x, (double*)y, 1.0, 0, s))
+                throw Error(EQC_E_STATE, "double-float apply unavailable");
             EQC_CUDA(cudaEventRecord(e1, s));
             EQC_CUDA(cudaEventSynchronize(e1));
             float t = 0;

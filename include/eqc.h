@@ -302,13 +302,14 @@ eqc_status eqc_damage_evolve(eqc_handle* h);
  * eqc_layout gives nx = 4*NelX+1, ny = 4*NelY+1 and the row pitch ld (elements). */
 eqc_status eqc_layout(eqc_handle* h, int64_t* nx, int64_t* ny, int64_t* ld);
 
-/* y = K x on device buffers in the internal layout, FP64 (dtype 0) or FP32
- * (dtype 1, W held in FP32), on the handle's stream.  Asynchronous. */
+/* y = K x on device buffers in the internal layout, FP64 (dtype 0), FP32 (dtype 1, W held in
+ * FP32) or FP64 vectors in double-float arithmetic (dtype 2: the mixed solver's true-residual
+ * apply, ~1e-14 relative), on the handle's stream.  Asynchronous. */
 eqc_status eqc_apply_K_device(eqc_handle* h, const void* x, void* y, int32_t dtype);
 
-/* Time nrep launches of the stiffness apply with CUDA events on the handle's
- * stream, flushing L2 between launches when flush_l2 != 0; *ms gets the mean
- * launch duration. */
+/* Time nrep launches of the stiffness apply (dtype as for eqc_apply_K_device) with CUDA
+ * events on the handle's stream, flushing L2 between launches when flush_l2 != 0; *ms gets
+ * the mean launch duration. */
 eqc_status eqc_time_apply(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t flush_l2, double* ms);
 
 /* Time nrep back-to-back launches of the stiffness apply rotating over ncopies replicas of its

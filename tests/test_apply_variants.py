@@ -78,3 +78,26 @@ def test_fused_vcycle_equals_separate_kernels(eqclib, monkeypatch, variant, prec
     for k in out[0][1]:
         assert np.array_equal(out[0][1][k], out[1][1][k]), k
 
+
+
+@pytest.mark.parametrize("name", ["homog48", "odd37x23", "dz480"])
+def test_double_float_apply_matches_fp64(eqclib, name):
+    """The double-float apply of the mixed solver's true residuals against the FP64 apply: on
+    random x to 1e-12 of max |K x|, and on a smooth field (K x small against |K| |x|, the
+    cancellation a residual has) to 1e-12 of the random case's scale."""
+    torch = pytest.importorskip("torch")
+    P = set_parameters(MESHES[name])
+    with Solver(P, precond=EQC_PC_JACOBI) as s:
+        nx, ny, ld = s.layout()
+        g = torch.Generator().manual_seed(11)
+        x = torch.zeros(ny, ld, dtype=torch.float64)
+        x[:, :nx] = torch.rand(ny, nx, generator=g, dtype=torch.float64) - 0.5
+        y64, ydf = _apply(s, torch, x, 0), _apply(s, torch, x, 2)
+        scale = np.max(np.abs(y64))
+        assert np.max(np.abs(ydf - y64)) <= 1e-12 * scale
+        xs = torch.zeros(ny, ld, dtype=torch.float64)
+        ix = torch.arange(nx, dtype=torch.float64)[None, :]
+        iy = torch.arange(ny, dtype=torch.float64)[:, None]
+        xs[:, :nx] = 0.3 + 1e-3 * ix + 2e-3 * iy + 1e-4 * torch.sin(0.05 * ix) * torch.cos(0.03 * iy)
+        z64, zdf = _apply(s, torch, xs, 0), _apply(s, torch, xs, 2)
+        assert np.max(np.abs(zdf - z64)) <= 1e-12 * scale * float(xs.abs().max()) / 0.5
