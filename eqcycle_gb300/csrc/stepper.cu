@@ -12,6 +12,7 @@
 #include "learn.h"
 #include "fault.cuh"
 #include "reduce.cuh"
+#include "vec.cuh"
 #include <cmath>
 #include <algorithm>
 #include <chrono>
@@ -141,20 +142,34 @@ __global__ void k_dyn_predict(double* __restrict__ d, double* __restrict__ v, co
 }
 
 // Mixed-precision predictor: the increment dd = dt v + dt^2/2 a in FP64, d += dd, dd32 = (float) dd.
-__global__ void k_dyn_predict_inc(double* __restrict__ d, double* __restrict__ v, const double* __restrict__ a,
-                                  double* __restrict__ vPre_f, float* __restrict__ dd32, int Nf, int64_t n, Ctrl* C) {
+// The mixed method's Newmark vector kernels are bound by GB300's FP64 issue rate, not by HBM:
+// 4-wide accesses and fused multiply-adds (this method does not reproduce the reference's
+// operation order; the plain method's kernels do).
+__global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d, double* __restrict__ v,
+                                                         const double* __restrict__ a, double* __restrict__ vPre_f,
+                                                         float* __restrict__ dd32, int Nf, int64_t n, Ctrl* C) {
     const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         C->r_valid = 0;
         C->qs_prev = 0;
     }
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double vi = v[i], ai = a[i];
-        if (i < Nf) vPre_f[i] = vi;
-        const double dd = dt * vi + hdt2 * ai;
-        d[i] = d[i] + dd;
-        dd32[i] = (float)dd;
-        v[i] = vi + hdt * ai;
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        double dd4[4], vv[4], aa[4];
+        float f[4];
+        ld4(d + i, dd4);
+        ld4(v + i, vv);
+        ld4(a + i, aa);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i + k < Nf) vPre_f[i + k] = vv[k];
+            const double inc = __fma_rn(dt, vv[k], __dmul_rn(hdt2, aa[k]));
+            dd4[k] = __dadd_rn(dd4[k], inc);
+            f[k] = (float)inc;
+            vv[k] = __fma_rn(hdt, aa[k], vv[k]);
+        }
+        st4(d + i, dd4);
+        st4(v + i, vv);
+        st4(dd32 + i, f);
     }
 }
 
@@ -170,16 +185,22 @@ __global__ void k_kd_select(Ctrl* C, cudaGraphConditionalHandle hf, cudaGraphCon
 }
 
 // a = -K d with K d either refreshed (Kd written by the FP64 apply) or Kd += K dd (t32, FP32).
-__global__ void k_dyn_force(double* __restrict__ Kd, const float* __restrict__ t32, double* __restrict__ a, int64_t n,
-                            Ctrl* C) {
+__global__ void __launch_bounds__(256) k_dyn_force(double* __restrict__ Kd, const float* __restrict__ t32,
+                                                   double* __restrict__ a, int64_t n, Ctrl* C) {
     const int full = C->kd_full;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double k = Kd[i];
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        double k[4];
+        ld4(Kd + i, k);
         if (!full) {
-            k += (double)t32[i];
-            Kd[i] = k;
+            float t[4];
+            ld4(t32 + i, t);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) k[q] = __dadd_rn(k[q], (double)t[q]);
+            st4(Kd + i, k);
         }
-        a[i] = -k;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) k[q] = -k[q];
+        st4(a + i, k);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         C->kd_valid = 1;
@@ -238,6 +259,24 @@ __global__ void k_dyn_correct(double* __restrict__ a, double* __restrict__ v, co
         const double ai = inv ? a[i] * M[i] : a[i] / M[i];
         a[i] = ai;
         v[i] = v[i] + hdt * ai;
+    }
+}
+// The mixed method's correction: a *= 1/M ; v += dt/2 a (4-wide, one multiply and one FMA).
+__global__ void __launch_bounds__(256) k_dyn_correct_inv(double* __restrict__ a, double* __restrict__ v,
+                                                         const double* __restrict__ invM, int64_t n, const Ctrl* C) {
+    const double hdt = C->half_dt;
+    for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        double aa[4], vv[4], mm[4];
+        ld4(a + i, aa);
+        ld4(v + i, vv);
+        ld4(invM + i, mm);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            aa[k] = __dmul_rn(aa[k], mm[k]);
+            vv[k] = __fma_rn(hdt, aa[k], vv[k]);
+        }
+        st4(a + i, aa);
+        st4(v + i, vv);
     }
 }
 
@@ -335,6 +374,8 @@ static FaultArgs fargs(Handle& h, const int* bcflag) {
 }
 
 static inline int vblocks(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4 * 152); }
+// 4 entries per thread: every SM's threads resident at once (8 CTAs of 256)
+static inline int vblocks4(int64_t n) { return (int)std::min<int64_t>((n / 4 + 255) / 256, 8 * 152); }
 
 static void launch_check() { EQC_CHECK_LAUNCH(); }
 
@@ -590,7 +631,7 @@ static void enqueue_dyn(Handle& h, bool graph) {
     FaultArgs f = fargs(h, h.bcflag.p);
     if (h.opt.precision == EQC_MIXED) {
         // FP64 accumulation of d and of K d, FP32 apply of the step's increment
-        k_dyn_predict_inc<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n, h.ctrl.p);
+        k_dyn_predict_inc<<<vblocks4(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n, h.ctrl.p);
         count_launch();
         if (graph) {
             const cudaGraphConditionalHandle hf = cond_handle(h), hi = cond_handle(h);
@@ -617,7 +658,7 @@ static void enqueue_dyn(Handle& h, bool graph) {
             if (full) apply_K<double>(h.d.p, h.Kd.p, args64(h), 1.0, 0, s);
             else apply_K<float>(h.g32.p, h.q32.p, args32(h), 1.0f, 0, s);
         }
-        k_dyn_force<<<vblocks(n), 256, 0, s>>>(h.Kd.p, h.q32.p, h.a.p, n, h.ctrl.p);
+        k_dyn_force<<<vblocks4(n), 256, 0, s>>>(h.Kd.p, h.q32.p, h.a.p, n, h.ctrl.p);
         count_launch();
     } else {
         k_dyn_predict<<<vblocks(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.F.Nf, n, h.ctrl.p);
@@ -628,7 +669,8 @@ static void enqueue_dyn(Handle& h, bool graph) {
                                 h.nBcT);
     k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
     const bool mixed = h.opt.precision == EQC_MIXED;
-    k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, mixed ? h.invM.p : h.M.p, n, h.ctrl.p, mixed ? 1 : 0);
+    if (mixed) k_dyn_correct_inv<<<vblocks4(n), 256, 0, s>>>(h.a.p, h.v.p, h.invM.p, n, h.ctrl.p);
+    else k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, h.M.p, n, h.ctrl.p, 0);
     count_launch(3);
     if (h.nCreep) {
         k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, h.a.p, nullptr);
