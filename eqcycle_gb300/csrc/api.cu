@@ -6,6 +6,7 @@
 #include <cstring>
 #include <cstdlib>
 #include <algorithm>
+#include <unordered_map>
 #include <chrono>
 
 namespace eqc {
@@ -241,6 +242,48 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     };
     std::vector<int64_t> lBcL = to_lay(m.iBcL, m.n_iBcL), lBcT = to_lay(m.iBcT, m.n_iBcT);
     std::vector<int64_t> lCreep = to_lay(m.FltIglobBC, m.n_FltIglobBC), lSeis = to_lay(m.out_seis, m.n_out_seis);
+    {   // per-node boundary operations (k_dyn_bc_nodes), nodes in first-appearance order
+        std::vector<int64_t> node;
+        std::vector<int> ops;
+        std::vector<double> cl, ct;
+        std::unordered_map<int64_t, size_t> at;
+        auto slot = [&](int64_t g) {
+            auto it = at.find(g);
+            if (it != at.end()) return it->second;
+            at[g] = node.size();
+            node.push_back(g);
+            ops.push_back(0);
+            cl.push_back(0.0);
+            ct.push_back(0.0);
+            return node.size() - 1;
+        };
+        for (int64_t g : lCreep) ops[slot(g)] |= 1;
+        bool dup = false;   // a node twice in the left or the top list: keep the list kernel
+        for (size_t k = 0; k < lBcL.size(); ++k) {
+            const size_t q = slot(lBcL[k]);
+            dup = dup || (ops[q] & 2);
+            ops[q] |= 2;
+            cl[q] = m.BcLC[k];
+        }
+        for (size_t k = 0; k < lBcT.size(); ++k) {
+            const size_t q = slot(lBcT[k]);
+            dup = dup || (ops[q] & 4);
+            ops[q] |= 4;
+            ct[q] = m.BcTC[k];
+        }
+        if (!dup && !node.empty()) {
+            h.bcNode.alloc(node.size());
+            h.bcNode.upload(node.data(), node.size(), s);
+            h.bcOps.alloc(ops.size());
+            h.bcOps.upload(ops.data(), ops.size(), s);
+            h.bcL.alloc(cl.size());
+            h.bcL.upload(cl.data(), cl.size(), s);
+            h.bcT.alloc(ct.size());
+            h.bcT.upload(ct.data(), ct.size(), s);
+            h.nBcNodes = (int)node.size();
+            EQC_CUDA(cudaStreamSynchronize(s));
+        }
+    }
     up_i(h.iBcL, lBcL);
     up_i(h.iBcT, lBcT);
     up_i(h.iCreep, lCreep);

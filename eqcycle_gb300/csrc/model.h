@@ -113,6 +113,12 @@ struct Handle {
     double Vpl = 0, Vthres = 0, Vevne = 0, dt0 = 0, Total_time = 0, yr2sec = 0;
     // reference numbering <-> layout
     std::vector<int64_t> ref2lay;    // [nglob] reference node (0-based) -> layout index
+    // the dynamic step's boundary operations per node of iCreep U iBcL U iBcT: bit 0 zero a,
+    // bit 1 subtract the left term, bit 2 the top term (k_dyn_bc's order)
+    DBuf<int64_t> bcNode;
+    DBuf<int> bcOps;
+    DBuf<double> bcL, bcT;
+    int nBcNodes = 0;
     DBuf<int64_t> d_ref2lay;
     // element data
     DBuf<double> W64, W64p;

@@ -145,13 +145,23 @@ __global__ void k_dyn_predict(double* __restrict__ d, double* __restrict__ v, co
 // The mixed method's Newmark vector kernels are bound by GB300's FP64 issue rate, not by HBM:
 // 4-wide accesses and fused multiply-adds (this method does not reproduce the reference's
 // operation order; the plain method's kernels do).
+// Its first thread also chooses how the step gets K d: a full FP64 apply (start of a dynamic phase,
+// every KD_REFRESH steps) or the FP32 apply of the increment (the two conditional bodies after it).
 __global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d, double* __restrict__ v,
                                                          const double* __restrict__ a, double* __restrict__ vPre_f,
-                                                         float* __restrict__ dd32, int Nf, int64_t n, Ctrl* C) {
+                                                         float* __restrict__ dd32, int Nf, int64_t n, Ctrl* C,
+                                                         cudaGraphConditionalHandle hf, cudaGraphConditionalHandle hi,
+                                                         int use_cond) {
     const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         C->r_valid = 0;
         C->qs_prev = 0;
+        const int full = (!C->kd_valid || C->kd_age >= KD_REFRESH) ? 1 : 0;
+        C->kd_full = full;
+        if (use_cond) {
+            cudaGraphSetConditional(hf, full ? 1u : 0u);
+            cudaGraphSetConditional(hi, full ? 0u : 1u);
+        }
     }
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double dd4[4], vv[4], aa[4];
@@ -173,16 +183,6 @@ __global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d,
     }
 }
 
-// Chooses how this step gets K d: a full FP64 apply (start of a dynamic phase, every KD_REFRESH
-// steps) or the FP32 apply of the increment.
-__global__ void k_kd_select(Ctrl* C, cudaGraphConditionalHandle hf, cudaGraphConditionalHandle hi, int use_cond) {
-    const int full = (!C->kd_valid || C->kd_age >= KD_REFRESH) ? 1 : 0;
-    C->kd_full = full;
-    if (use_cond) {
-        cudaGraphSetConditional(hf, full ? 1u : 0u);
-        cudaGraphSetConditional(hi, full ? 0u : 1u);
-    }
-}
 
 // a = -K d with K d either refreshed (Kd written by the FP64 apply) or Kd += K dd (t32, FP32).
 __global__ void __launch_bounds__(256) k_dyn_force(double* __restrict__ Kd, const float* __restrict__ t32,
@@ -216,6 +216,22 @@ __global__ void k_dyn_bc(double* __restrict__ a, const double* __restrict__ v, c
     for (int k = threadIdx.x; k < nL; k += blockDim.x) a[iL[k]] = a[iL[k]] - CL[k] * v[iL[k]];
     __syncthreads();
     for (int k = threadIdx.x; k < nT; k += blockDim.x) a[iT[k]] = a[iT[k]] - CT[k] * v[iT[k]];
+}
+
+// The same boundary operations over the union of the three lists, one thread per node, each
+// node's operations in k_dyn_bc's order (zero, left term, top term): many CTAs instead of one.
+__global__ void k_dyn_bc_nodes(double* __restrict__ a, const double* __restrict__ v, const int64_t* __restrict__ node,
+                               const int* __restrict__ ops, const double* __restrict__ cl, const double* __restrict__ ct,
+                               int n) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += blockDim.x * gridDim.x) {
+        const int64_t i = node[k];
+        const int op = ops[k];
+        double ai = a[i];
+        if (op & 1) ai = 0.;
+        if (op & 2) ai = ai - cl[k] * v[i];
+        if (op & 4) ai = ai - ct[k] * v[i];
+        a[i] = ai;
+    }
 }
 
 // Fault boundary condition (main.jl:321-331): FltVfree, Vf, FBC! (two NR solves per node),
@@ -631,11 +647,10 @@ static void enqueue_dyn(Handle& h, bool graph) {
     FaultArgs f = fargs(h, h.bcflag.p);
     if (h.opt.precision == EQC_MIXED) {
         // FP64 accumulation of d and of K d, FP32 apply of the step's increment
-        k_dyn_predict_inc<<<vblocks4(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n, h.ctrl.p);
-        count_launch();
         if (graph) {
             const cudaGraphConditionalHandle hf = cond_handle(h), hi = cond_handle(h);
-            k_kd_select<<<1, 1, 0, s>>>(h.ctrl.p, hf, hi, 1);
+            k_dyn_predict_inc<<<vblocks4(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n,
+                                                          h.ctrl.p, hf, hi, 1);
             count_launch();
             const int64_t t0 = capture_tally();
             cond_begin(h, cudaGraphCondTypeIf, hf);
@@ -650,7 +665,8 @@ static void enqueue_dyn(Handle& h, bool graph) {
                 h.capturing->k_fixed_extra += std::max(t1 - t0, capture_tally() - t1);   // one of the two runs
             }
         } else {
-            k_kd_select<<<1, 1, 0, s>>>(h.ctrl.p, 0, 0, 0);
+            k_dyn_predict_inc<<<vblocks4(n), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n,
+                                                          h.ctrl.p, 0, 0, 0);
             count_launch();
             int full = 0;
             EQC_CUDA(cudaMemcpyAsync(&full, &h.ctrl.p->kd_full, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -665,8 +681,12 @@ static void enqueue_dyn(Handle& h, bool graph) {
         count_launch();
         apply_K<double>(h.d.p, h.a.p, args64(h), -1.0, 0, s);
     }
-    k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p, h.BcTC.p,
-                                h.nBcT);
+    if (h.nBcNodes > 0)
+        k_dyn_bc_nodes<<<(h.nBcNodes + 127) / 128, 128, 0, s>>>(h.a.p, h.v.p, h.bcNode.p, h.bcOps.p, h.bcL.p, h.bcT.p,
+                                                               h.nBcNodes);
+    else
+        k_dyn_bc<<<1, 1024, 0, s>>>(h.a.p, h.v.p, h.iCreep.p, h.nCreep, h.iBcL.p, h.BcLC.p, h.nBcL, h.iBcT.p, h.BcTC.p,
+                                    h.nBcT);
     k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
     const bool mixed = h.opt.precision == EQC_MIXED;
     if (mixed) k_dyn_correct_inv<<<vblocks4(n), 256, 0, s>>>(h.a.p, h.v.p, h.invM.p, n, h.ctrl.p);
