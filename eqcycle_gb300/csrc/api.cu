@@ -310,6 +310,8 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     while (nfbc < Nf && creep[nfbc]) ++nfbc;
     for (int k = nfbc; k < Nf; ++k) fail_if(creep[k], "creeping fault nodes must be the deepest ones");
     F.NFBC0 = nfbc;
+    h.creep_prefix = true;
+    for (auto g : lCreep) h.creep_prefix = h.creep_prefix && g < nfbc;
     for (DBuf<double>* b : {&F.fo, &F.Vo, &F.xLf, &F.cca, &F.ccb, &F.Seff, &F.tauo, &F.XiLf, &F.FltB, &F.FltZ, &F.FltX,
                             &F.Mf, &F.psi, &F.psi1, &F.psi2, &F.tau, &F.tau1, &F.tau2, &F.Vf, &F.Vf0, &F.Vf1, &F.Vf2,
                             &F.FltVfree, &F.vPre, &F.Flast})

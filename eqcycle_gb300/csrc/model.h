@@ -119,6 +119,7 @@ struct Handle {
     DBuf<int> bcOps;
     DBuf<double> bcL, bcT;
     int nBcNodes = 0;
+    bool creep_prefix = false;   // iCreep lies in the fault row (its nodes: the prefix [0, NFBC0))
     DBuf<int64_t> d_ref2lay;
     // element data
     DBuf<double> W64, W64p;

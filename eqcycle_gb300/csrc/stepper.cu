@@ -277,9 +277,11 @@ __global__ void k_dyn_correct(double* __restrict__ a, double* __restrict__ v, co
         v[i] = v[i] + hdt * ai;
     }
 }
-// The mixed method's correction: a *= 1/M ; v += dt/2 a (4-wide, one multiply and one FMA).
+// The mixed method's correction: a *= 1/M ; v += dt/2 a (4-wide, one multiply and one FMA); the
+// first nzero nodes (the creeping fault nodes, a prefix of the fault row) end with a = v = 0.
 __global__ void __launch_bounds__(256) k_dyn_correct_inv(double* __restrict__ a, double* __restrict__ v,
-                                                         const double* __restrict__ invM, int64_t n, const Ctrl* C) {
+                                                         const double* __restrict__ invM, int64_t n, const Ctrl* C,
+                                                         int64_t nzero) {
     const double hdt = C->half_dt;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double aa[4], vv[4], mm[4];
@@ -290,6 +292,7 @@ __global__ void __launch_bounds__(256) k_dyn_correct_inv(double* __restrict__ a,
         for (int k = 0; k < 4; ++k) {
             aa[k] = __dmul_rn(aa[k], mm[k]);
             vv[k] = __fma_rn(hdt, aa[k], vv[k]);
+            if (i + k < nzero) aa[k] = vv[k] = 0.0;
         }
         st4(a + i, aa);
         st4(v + i, vv);
@@ -689,10 +692,12 @@ static void enqueue_dyn(Handle& h, bool graph) {
                                     h.nBcT);
     k_dyn_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.a.p, h.v.p, f, h.ctrl.p);
     const bool mixed = h.opt.precision == EQC_MIXED;
-    if (mixed) k_dyn_correct_inv<<<vblocks4(n), 256, 0, s>>>(h.a.p, h.v.p, h.invM.p, n, h.ctrl.p);
+    const bool zero_fused = mixed && h.creep_prefix;
+    if (mixed) k_dyn_correct_inv<<<vblocks4(n), 256, 0, s>>>(h.a.p, h.v.p, h.invM.p, n, h.ctrl.p,
+                                                            zero_fused ? (int64_t)h.F.NFBC0 : 0);
     else k_dyn_correct<<<vblocks(n), 256, 0, s>>>(h.a.p, h.v.p, h.M.p, n, h.ctrl.p, 0);
     count_launch(3);
-    if (h.nCreep) {
+    if (h.nCreep && !zero_fused) {
         k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.v.p, h.a.p, nullptr);
         count_launch();
     }
