@@ -1,7 +1,7 @@
 """GPU parity: libeqc (through the C ABI) against the CPU oracle on the same inputs.
 
 Tolerances (FP64 paths):
-  * stiffness apply: 1e-12 relative (max-norm), the benchmark spec's bound for K x;
+  * stiffness apply: 1e-12 relative (max-norm), the bound required of K x;
   * quasi-static solve: both sides solved to a 1e-13 relative residual, solutions agree to
     1e-10 relative (forward error is bounded by cond(K_II) x residual);
   * friction kernels: 1e-12 relative (CUDA vs libm exp/log differ by ulps);
