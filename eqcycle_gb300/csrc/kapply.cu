@@ -5,14 +5,19 @@
 //     a_e = c1 * H * (W_e .* (H' u_e)) + c2 * (W_e .* (u_e H)) * H'
 // scattered through the connectivity (the Conn product of src/PCG.jl:266).
 //
-// GB300 design.  The mesh is structured, so node indices are computed, not loaded.
-// One CTA owns a tile of TEX x TEY elements' worth of nodes and gathers, for each
-// owned node, the contributions of the <= 4 elements containing it in a fixed order
-// (deterministic, no atomics, bitwise reproducible).  The owned node range of a tile
-// is [4*ex0, 4*(ex0+TEX)) x [4*ey0, 4*(ey0+TEY)); the elements just left of and below
-// the tile are recomputed as a halo.  Per element the work is split into 5 x-lines
-// and 5 y-lines (sum factorisation: two 5x5 contractions per line) staged through
-// shared memory.
+// GB300 design.  The mesh is structured, so node indices are computed, not loaded; every
+// node sums its element contributions in a fixed order (deterministic, no atomics, bitwise
+// reproducible).  Per element the work is 5 x-lines and 5 y-lines (sum factorisation: two
+// 5-point contractions per line).  Kernels, by apply_variant:
+//   k_apply_rows   FP32, one lane per element, one warp per element row, ROWS rows per CTA
+//                  plus a halo warp (variants 0, 4-7; the FP32 default);
+//   k_apply_walk   the same arithmetic fed by TMA, one wave of CTAs each walking up a strip
+//                  (variant 8; the autotuner's usual choice);
+//   k_apply_pipe   persistent tiles with a TMA pipeline, node-line form (the FP64 default,
+//                  FP32 variant 3); k_apply_tma / k_apply_lines: one tile per CTA (1, 2);
+//   k_apply        the strip modes 2 and 3 (first element row only).
+// The FP32 element kernels take an epilogue (epi.cuh) that finishes the V-cycle's residual or
+// Chebyshev step at each owned node.
 #include "model.h"
 #include "vec.cuh"
 #include "epi.cuh"
