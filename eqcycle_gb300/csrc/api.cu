@@ -2,6 +2,7 @@
 // permutation, host-array entry points.
 #include "model.h"
 #include "learn.h"
+#include "host_par.h"
 #include <cmath>
 #include <cstring>
 #include <cstdlib>
@@ -176,10 +177,15 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     auto t0 = clk::now();
 
     // reference node -> layout index, from the connectivity (or MeshBox's numbering rule)
-    h.ref2lay.assign(m.nglob, -1);
-    if (mat) {
-        for (int64_t iy = 0; iy < L.ny; ++iy)
+    h.ref2lay.resize(m.nglob);
+    constexpr int64_t CH = 1 << 16;
+    parallel_for((m.nglob + CH - 1) / CH, [&](int64_t c) {
+        std::fill(h.ref2lay.begin() + c * CH, h.ref2lay.begin() + std::min(m.nglob, (c + 1) * CH), (int64_t)-1);
+    });
+    if (mat) {   // MeshBox's numbering is a bijection of the nx x ny nodes: rows write disjoint entries
+        parallel_for(L.ny, [&](int64_t iy) {
             for (int64_t ix = 0; ix < L.nx; ++ix) h.ref2lay[meshbox_id(ix, iy, L.nx)] = iy * L.ld + ix;
+        });
     }
     for (int64_t e = 0; e < (mat ? 0 : m.Nel); ++e) {
         const int ex = (int)(e % m.NelX), ey = (int)(e / m.NelX);
@@ -192,7 +198,14 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
                 h.ref2lay[ref] = lay;
             }
     }
-    for (int64_t g = 0; g < m.nglob; ++g) fail_if(h.ref2lay[g] < 0, "iglob does not cover every node");
+    {
+        const int64_t nc = (m.nglob + CH - 1) / CH;
+        std::vector<char> hole(nc, 0);
+        parallel_for(nc, [&](int64_t c) {
+            for (int64_t g = c * CH; g < std::min(m.nglob, (c + 1) * CH); ++g) hole[c] |= h.ref2lay[g] < 0;
+        });
+        for (char x : hole) fail_if(x != 0, "iglob does not cover every node");
+    }
     const int Nf = (int)m.FltNglob;
     for (int k = 0; k < Nf; ++k)
         fail_if(h.ref2lay[m.iFlt[k] - 1] != k, "iFlt must run along the y = 0 edge from x = -LX (BoundaryMatrix 'B')");

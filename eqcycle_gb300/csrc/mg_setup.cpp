@@ -4,26 +4,9 @@
 #include "mg.h"
 #include <cmath>
 #include <algorithm>
-#include <thread>
+#include "host_par.h"
 
 namespace eqc {
-
-// f(i) for i in [0, n) on the host's cores, in contiguous chunks; callers write disjoint outputs,
-// so the result does not depend on the thread count.
-template <class F>
-static void parallel_for(int64_t n, F&& f) {
-    const int64_t nt = std::max<int64_t>(1, std::min<int64_t>(std::thread::hardware_concurrency(), n / 16 + 1));
-    if (nt <= 1) {
-        for (int64_t i = 0; i < n; ++i) f(i);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int64_t t = 0; t < nt; ++t)
-        th.emplace_back([&, t] {
-            for (int64_t i = n * t / nt; i < n * (t + 1) / nt; ++i) f(i);
-        });
-    for (std::thread& x : th) x.join();
-}
 
 static void finish_restriction(Transfer1D& t) {
     t.r_ptr.assign(t.nc + 1, 0);
