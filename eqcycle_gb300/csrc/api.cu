@@ -614,6 +614,7 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         else if (s == "setup_ms_nodes") *out = h.setup_ms[2];
         else if (s == "setup_ms_other") *out = h.setup_ms[3];
         else if (s == "setup_ms_hierarchy") *out = h.setup_ms[4];
+        else if (s == "pdl_edges") *out = (double)h.pdl_edges;
         else if (s == "reliable_delta") *out = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : 1e-3;
         else if (s == "dt") *out = C.dt;
         else if (s == "isolver") *out = C.isolver;

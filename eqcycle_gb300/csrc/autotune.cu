@@ -15,6 +15,7 @@ namespace eqc {
 // d0 = d with the fault row moved to the next step's first F = d + v dt (src/main.jl:231-238)
 __global__ void k_trial_rhs(const double* __restrict__ d, const double* __restrict__ v, double* __restrict__ d0,
                             int64_t n, int Nf, const Ctrl* C) {
+    EQC_GRID_WAIT();
     const double dt = C->dt;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         d0[i] = (i < Nf) ? d[i] + v[i] * dt : d[i];
@@ -30,6 +31,7 @@ static double trial(Handle& h, const double* d0, int reps, int* iters) {
         EQC_CUDA(cudaMemcpyAsync(h.d.p, d0, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         enqueue_solve(h, h.opt.cg_tol, h.opt.cg_maxit, true, false, nullptr);
         EQC_CUDA(cudaStreamEndCapture(s, &g));
+        make_programmatic(g);
     } catch (...) {
         abort_capture(h);
         throw;

@@ -16,6 +16,7 @@ int64_t g_launches = 0;
 template <class T>
 __global__ void __launch_bounds__(VEC_THREADS) k_dot(const T* __restrict__ x, const T* __restrict__ y, int64_t n,
                                                      double* part, unsigned* count, double* out) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     DotAcc<T> acc;
     const int64_t n4 = n & ~(int64_t)3;

@@ -28,6 +28,16 @@ struct Error : std::runtime_error {
 
 #define EQC_CHECK_LAUNCH() EQC_CUDA(cudaGetLastError())
 
+// First statement of every kernel: wait until the grids this launch depends on have completed
+// and their memory is visible.  A no-op for an ordinary launch; in the step graphs, edges
+// between consecutive kernels are programmatic (make_programmatic), so a kernel's CTAs are
+// scheduled while its predecessor is still running and start work as soon as it finishes.
+#if defined(__CUDA_ARCH__)
+#define EQC_GRID_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+#else
+#define EQC_GRID_WAIT() do {} while (0)
+#endif
+
 // ---- device buffer ----------------------------------------------------------------
 template <class T>
 struct DBuf {

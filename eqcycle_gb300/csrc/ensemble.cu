@@ -12,6 +12,7 @@
 namespace eqc {
 
 __global__ void k_regime_select(const Ctrl* C, cudaGraphConditionalHandle hq, cudaGraphConditionalHandle hd) {
+    EQC_GRID_WAIT();
     const unsigned q = C->isolver == 1 ? 1u : 0u;
     cudaGraphSetConditional(hq, q);
     cudaGraphSetConditional(hd, 1u - q);
@@ -75,6 +76,7 @@ static void ensemble_capture(eqc_ensemble& E) {
             EQC_CUDA(cudaStreamWaitEvent(s0, E.ev[1 + m], 0));    // join
         }
         EQC_CUDA(cudaStreamEndCapture(s0, &E.graph));
+        make_programmatic(E.graph);
     } catch (...) {
         for (Handle* hp : E.mem) {
             hp->capturing = nullptr;

@@ -7,6 +7,8 @@
 // (cudaGraphSetConditional), so a solve needs no host round trip.  The reliable update of
 // the mixed-precision solver is a conditional IF node inside that body.
 #include "model.h"
+#include <cstdlib>
+#include <cstring>
 
 namespace eqc {
 
@@ -73,10 +75,49 @@ void abort_capture(Handle& h) {
     capture_counting(false);
 }
 
+static bool own_kernel(cudaGraphNode_t n) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(n, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) return false;
+    cudaKernelNodeParams p{};
+    if (cudaGraphKernelNodeGetParams(n, &p) != cudaSuccess || !p.func) return false;
+    cudaLaunchAttributeValue cl{};   // cluster launches keep ordinary edges
+    if (cudaGraphKernelNodeGetAttribute(n, cudaLaunchAttributeClusterDimension, &cl) == cudaSuccess &&
+        (size_t)cl.clusterDim.x * cl.clusterDim.y * cl.clusterDim.z > 1)
+        return false;
+    const char* name = nullptr;
+    if (cudaFuncGetName(&name, p.func) != cudaSuccess || !name) return false;
+    return std::strncmp(name, "_ZN3eqc", 7) == 0 || std::strstr(name, "eqc::") != nullptr;
+}
+
+int64_t make_programmatic(cudaGraph_t g) {
+    if (std::getenv("EQC_NO_PDL") || !g) return 0;
+    size_t n = 0;
+    EQC_CUDA(cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &n));
+    if (n == 0) return 0;
+    std::vector<cudaGraphNode_t> from(n), to(n);
+    std::vector<cudaGraphEdgeData> ed(n);
+    EQC_CUDA(cudaGraphGetEdges(g, from.data(), to.data(), ed.data(), &n));
+    std::unordered_map<cudaGraphNode_t, int> indeg;
+    for (size_t i = 0; i < n; ++i) indeg[to[i]] += 1;
+    int64_t changed = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (ed[i].type != cudaGraphDependencyTypeDefault || ed[i].from_port != cudaGraphKernelNodePortDefault) continue;
+        if (indeg[to[i]] != 1 || !own_kernel(from[i]) || !own_kernel(to[i])) continue;
+        EQC_CUDA(cudaGraphRemoveDependencies(g, &from[i], &to[i], &ed[i], 1));
+        cudaGraphEdgeData pe{};
+        pe.from_port = cudaGraphKernelNodePortLaunchCompletion;
+        pe.type = cudaGraphDependencyTypeProgrammatic;
+        EQC_CUDA(cudaGraphAddDependencies(g, &from[i], &to[i], &pe, 1));
+        ++changed;
+    }
+    return changed;
+}
+
 void cond_end(Handle& h) {
     if (h.stream_stack.empty()) throw Error(EQC_E_STATE, "cond_end without cond_begin");
     cudaGraph_t g = nullptr;
     EQC_CUDA(cudaStreamEndCapture(h.stream, &g));
+    h.pdl_edges += make_programmatic(g);
     h.stream = h.stream_stack.back();
     h.stream_stack.pop_back();
 }

@@ -44,6 +44,7 @@ template <> __device__ __forceinline__ float Hc<float>(int i, int j) { return cH
 template <class T, int TEX, int TEY>
 __global__ void __launch_bounds__(256) k_apply(const T* __restrict__ x, T* __restrict__ y, ApplyArgs<T> A,
                                                T sign, int mode) {
+    EQC_GRID_WAIT();
     const Layout L = A.L;
     const bool strip = mode >= 2;
     const int ex0 = blockIdx.x * TEX;
@@ -266,6 +267,7 @@ __device__ __forceinline__ void lines_compute(const T* __restrict__ us, const T*
 template <class T, int TEX, int TEY, int NT>
 __global__ void __launch_bounds__(NT) k_apply_lines(const T* __restrict__ x, T* __restrict__ y, ApplyArgs<T> A,
                                                     T sign, int zero_row0) {
+    EQC_GRID_WAIT();
     const Layout L = A.L;
     constexpr int UX = 4 * TEX + 5, UY = 4 * TEY + 5;   // node tile incl. one halo element
     constexpr int OX = 4 * TEX, OY = 4 * TEY;           // owned nodes
@@ -354,6 +356,7 @@ template <class T, int TEX, int TEY, int NT>
 __global__ void __launch_bounds__(NT) k_apply_tma(const __grid_constant__ CUtensorMap umap,
                                                   const __grid_constant__ CUtensorMap wmap, T* __restrict__ y,
                                                   ApplyArgs<T> A, T sign, int zero_row0) {
+    EQC_GRID_WAIT();
     constexpr int UY = 4 * TEY + 5;
     constexpr int OX = 4 * TEX, OY = 4 * TEY;
     constexpr int EX = TEX + 1, EY = TEY + 1;
@@ -408,6 +411,7 @@ template <class T, int TEX, int TEY, int NT>
 __global__ void __launch_bounds__(NT) k_apply_pipe(const __grid_constant__ CUtensorMap umap,
                                                    const __grid_constant__ CUtensorMap wmap, T* __restrict__ y,
                                                    ApplyArgs<T> A, T sign, int zero_row0, int ntx, int ntiles) {
+    EQC_GRID_WAIT();
     using PL = PipeLayout<T, TEX, TEY>;
     extern __shared__ __align__(128) unsigned char smem[];
     T* ys = reinterpret_cast<T*>(smem + PSTAGES * PL::STAGE);
@@ -623,6 +627,7 @@ template <int ROWS, int MINB>
 __global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const float* __restrict__ x, float* __restrict__ y,
                                                                      ApplyArgs<float> A, float sign, int zero_row0,
                                                                      OpEpi<float> E) {
+    EQC_GRID_WAIT();
     const Layout L = A.L;
     __shared__ float Ts[ROWS + 1][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -722,6 +727,7 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
                                                                 const __grid_constant__ CUtensorMap wmap,
                                                                 float* __restrict__ y, ApplyArgs<float> A, float sign,
                                                                 int zero_row0, int nsx, int rw, OpEpi<float> E) {
+    EQC_GRID_WAIT();
     extern __shared__ __align__(128) unsigned char smem[];
     const Layout L = A.L;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

@@ -41,6 +41,7 @@ template <int ROWS>
 __global__ void __launch_bounds__(32 * (ROWS + 1), 2)
     k_apply_df(const double* __restrict__ x, double* __restrict__ y, const float* __restrict__ Whi,
                const float* __restrict__ Wlo, Layout L, df c1, df c2, double sign, int zero_row0) {
+    EQC_GRID_WAIT();
     __shared__ float Th[ROWS + 1][5][32], Tl[ROWS + 1][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int ex = (int)blockIdx.x * 31 - 1 + lane;

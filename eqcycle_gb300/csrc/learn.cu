@@ -25,6 +25,7 @@ template <class TA, class TB>
 __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const TA* __restrict__ A, int64_t sam, int64_t sak,
                                               const TB* __restrict__ B, int64_t sbk, int64_t sbn, float* __restrict__ C,
                                               int64_t ldc, const float* __restrict__ bias, float* __restrict__ Cg) {
+    EQC_GRID_WAIT();
     __shared__ float As[16][65];
     __shared__ float Bs[16][65];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -90,6 +91,7 @@ template <int BMAX>
 __global__ void __launch_bounds__(256) k_gemv(int B, int N, int K, const float* __restrict__ x,
                                               const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
                                               float* __restrict__ y, float* __restrict__ yg) {
+    EQC_GRID_WAIT();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= N) return;
     const __nv_bfloat16* w = W + (int64_t)warp * K;
@@ -143,6 +145,7 @@ static void linear(int B, int N, int K, const float* x, const __nv_bfloat16* W, 
 __global__ void k_conv_fwd(const float* __restrict__ in, int Cin, int Tin, const __nv_bfloat16* __restrict__ W,
                            const float* __restrict__ bias, float* __restrict__ z, float* __restrict__ a, int Tout,
                            int B) {
+    EQC_GRID_WAIT();
     const int64_t n = (int64_t)B * GN_C * Tout;
     for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (int64_t)gridDim.x * blockDim.x) {
         const int t = (int)(idx % Tout);
@@ -166,6 +169,7 @@ __global__ void k_conv_fwd(const float* __restrict__ in, int Cin, int Tin, const
 // g_in[b][ci][s] = sum_{co,k : 2t+k-2 = s} W[co][ci][k] g_z[b][co][t]
 __global__ void k_conv_dgrad(const float* __restrict__ gz, int Tout, const __nv_bfloat16* __restrict__ W, int Cin,
                              float* __restrict__ gin, int Tin, int B) {
+    EQC_GRID_WAIT();
     const int64_t n = (int64_t)B * Cin * Tin;
     for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (int64_t)gridDim.x * blockDim.x) {
         const int s = (int)(idx % Tin);
@@ -188,6 +192,7 @@ __global__ void k_conv_dgrad(const float* __restrict__ gz, int Tout, const __nv_
 // gW[co][ci][k] = sum_{b,t} g_z[b][co][t] in[b][ci][2t+k-2] ; one CTA per (co, ci)
 __global__ void __launch_bounds__(256) k_conv_wgrad(const float* __restrict__ gz, const float* __restrict__ in, int Cin,
                                                     int Tin, int Tout, int B, float* __restrict__ gW) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     const int co = blockIdx.x / Cin, ci = blockIdx.x % Cin;
     float acc[GN_K] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -210,6 +215,7 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(const float* __restrict__ gz
 
 // out[c] = sum over rows r and positions t of g[r][c][t]   (bias gradients; T = 1 for fc)
 __global__ void __launch_bounds__(256) k_bias_grad(const float* __restrict__ g, int B, int Cn, int T, float* __restrict__ out) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     const int c = blockIdx.x;
     double s = 0.0;
@@ -223,6 +229,7 @@ __global__ void __launch_bounds__(256) k_bias_grad(const float* __restrict__ g, 
 
 // g *= GELU'(z)
 __global__ void k_gelu_bwd(float* __restrict__ g, const float* __restrict__ z, int64_t n) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         g[i] *= gelu_grad(z[i]);
 }
@@ -230,6 +237,7 @@ __global__ void k_gelu_bwd(float* __restrict__ g, const float* __restrict__ z, i
 // Mean squared error over B x nout: g = 2 (out - tgt) / (B nout); loss[b] = sum_j (out - tgt)^2
 __global__ void __launch_bounds__(256) k_mse(const float* __restrict__ out, const float* __restrict__ tgt, int nout, int B,
                                              float* __restrict__ g, double* __restrict__ loss) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     const int b = blockIdx.x;
     const float sc = 2.f / ((float)B * (float)nout);
@@ -245,6 +253,7 @@ __global__ void __launch_bounds__(256) k_mse(const float* __restrict__ out, cons
 
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
                        int64_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float gi = g[i];
         const float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -256,6 +265,7 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 }
 
 __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, int64_t n) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] = __float2bfloat16_rn(x[i]);
 }
@@ -428,6 +438,7 @@ struct GllFrac {
 // d[i] += s * P(out) and g32[i] = that increment, rows >= 1 (P bilinear from the coarse grid)
 __global__ void k_guess_prolong(const float* __restrict__ out, const float* __restrict__ scale, double* __restrict__ d,
                                 float* __restrict__ g32, Layout L, GllFrac f) {
+    EQC_GRID_WAIT();
     const float sc = scale[0];
     const int64_t n = L.size();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -450,6 +461,7 @@ __global__ void k_guess_prolong(const float* __restrict__ out, const float* __re
 __global__ void __launch_bounds__(1024) k_guess_features(const double* __restrict__ d, const double* __restrict__ dPre,
                                                          const double* __restrict__ Vf0, int Nf, double Vpl,
                                                          float* __restrict__ feat, float* __restrict__ scale) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     __shared__ double smax;
     double m = 0.0;
@@ -477,6 +489,7 @@ __global__ void __launch_bounds__(1024) k_guess_features(const double* __restric
 __global__ void k_guess_log(const float* __restrict__ feat, const float* __restrict__ scale, const double* __restrict__ d,
                             const double* __restrict__ dPre, Layout L, GllFrac f, int Nf, float* __restrict__ log_in,
                             float* __restrict__ log_tgt, const long long* __restrict__ count, long long cap) {
+    EQC_GRID_WAIT();
     const long long c = *count;
     if (c >= cap) return;
     const float sc = scale[0];
@@ -502,6 +515,7 @@ __global__ void k_guess_log(const float* __restrict__ feat, const float* __restr
     }
 }
 __global__ void k_guess_log_commit(long long* count, long long cap) {
+    EQC_GRID_WAIT();
     if (*count < cap) *count += 1;
 }
 
@@ -541,6 +555,7 @@ void gn_enqueue_log(Handle& h) {
 // x0[b] = pin[idx[b]], tgt[b] = ptgt[idx[b]]
 __global__ void k_gather_batch(const float* __restrict__ pin, const float* __restrict__ ptgt, const int* __restrict__ idx,
                                int B, int nin, int nout, float* __restrict__ x0, float* __restrict__ tgt) {
+    EQC_GRID_WAIT();
     const int64_t n = (int64_t)B * (nin + nout);
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         const int b = (int)(e / (nin + nout)), j = (int)(e % (nin + nout));
@@ -550,6 +565,7 @@ __global__ void k_gather_batch(const float* __restrict__ pin, const float* __res
     }
 }
 __global__ void k_sum_loss(const double* __restrict__ loss, int B, double* acc) {
+    EQC_GRID_WAIT();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double s = 0.0;
         for (int b = 0; b < B; ++b) s += loss[b];

@@ -12,6 +12,7 @@ namespace eqc {
 template <class T>
 __global__ void k_stencil(const T* __restrict__ A, const T* __restrict__ x, T* __restrict__ y, int cx, int cy,
                           OpEpi<T> E) {
+    EQC_GRID_WAIT();
     const int64_t N = (int64_t)cx * cy;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % cx), iy = (int)(i / cx);
@@ -32,6 +33,7 @@ template <class T>
 __global__ void k_prolong_add(const T* __restrict__ xc, T* __restrict__ xf, int nfx, int nfy, int ldf, int ldc,
                               const int* __restrict__ px, const int* __restrict__ py, const T* __restrict__ wx,
                               const T* __restrict__ wy) {
+    EQC_GRID_WAIT();
     const int64_t N = (int64_t)nfx * nfy;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % nfx), iy = (int)(i / nfx);
@@ -76,6 +78,7 @@ __global__ void k_restrict(const T* __restrict__ rf, T* __restrict__ bc, int ncx
                            const int* __restrict__ rpx, const int* __restrict__ rix, const T* __restrict__ rwx,
                            const int* __restrict__ rpy, const int* __restrict__ riy, const T* __restrict__ rwy,
                            ChebFirst<T> F) {
+    EQC_GRID_WAIT();
     const int64_t N = (int64_t)ncx * ncy;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int cxi = (int)(i % ncx), cyi = (int)(i / ncx);
@@ -108,6 +111,7 @@ struct GllW {
 // the thread of the last element column also takes the lattice's last node.
 template <class T>
 __global__ void k_prolong_sem(const T* __restrict__ xc, T* __restrict__ xf, Layout L, int ldc, GllW<T> w) {
+    EQC_GRID_WAIT();
     const int ex = blockIdx.x * blockDim.x + threadIdx.x;
     const int iy = blockIdx.y + 1;
     if (ex >= L.NelX || iy >= L.ny) return;
@@ -127,6 +131,7 @@ __global__ void k_prolong_sem(const T* __restrict__ xc, T* __restrict__ xf, Layo
 template <class T>
 __global__ void k_restrict_sem(const T* __restrict__ rf, T* __restrict__ bc, Layout L, int ldc, GllW<T> w,
                                ChebFirst<T> F) {
+    EQC_GRID_WAIT();
     const int vx = blockIdx.x * blockDim.x + threadIdx.x;
     const int vy = blockIdx.y;
     const int ncx = L.NelX + 1;
@@ -158,6 +163,7 @@ __global__ void k_restrict_sem(const T* __restrict__ rf, T* __restrict__ bc, Lay
 template <class T>
 __global__ void k_cheb_first(T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, const T* __restrict__ b,
                              const T* __restrict__ t, const T* __restrict__ Dinv, int64_t n, T inv_theta, int with_x) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const T ri = with_x ? mul_rn<T>(Dinv[i], sub_rn<T>(b[i], t[i])) : mul_rn<T>(Dinv[i], b[i]);
         const T di = mul_rn<T>(ri, inv_theta);
@@ -170,6 +176,7 @@ __global__ void k_cheb_first(T* __restrict__ x, T* __restrict__ r, T* __restrict
 template <class T>
 __global__ void k_cheb_step(T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, const T* __restrict__ t,
                             const T* __restrict__ Dinv, int64_t n, T c1, T c2) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         T ri = r[i], di = d[i], xi = x[i];
         cheb_step_pt<T>(ri, di, xi, t[i], Dinv[i], c1, c2);
@@ -181,6 +188,7 @@ __global__ void k_cheb_step(T* __restrict__ x, T* __restrict__ r, T* __restrict_
 // r = b - t
 template <class T>
 __global__ void k_sub(const T* __restrict__ b, const T* __restrict__ t, T* __restrict__ r, int64_t n) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         r[i] = b[i] - t[i];
 }
@@ -194,6 +202,7 @@ __device__ __forceinline__ T warp_sum_t(T v) {
 }
 template <class T>
 __global__ void k_dense_mv(const T* __restrict__ Cinv, const T* __restrict__ b, T* __restrict__ x, int n, int off) {
+    EQC_GRID_WAIT();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= n) return;
     const T* row = Cinv + (int64_t)warp * n;
@@ -209,11 +218,13 @@ __global__ void k_dense_mv(const T* __restrict__ Cinv, const T* __restrict__ b, 
 }
 template <class T>
 __global__ void k_scale(T* x, int64_t n, double s) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = (T)((double)x[i] * s);
 }
 template <class T>
 __global__ void k_mul(const T* a, T* x, int64_t n) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = a[i] * x[i];
 }

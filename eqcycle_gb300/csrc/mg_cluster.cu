@@ -50,6 +50,7 @@ __device__ __forceinline__ T stencil_at(const T* __restrict__ A, const T* x, int
 
 template <class T>
 __global__ void __launch_bounds__(1024, 1) k_coarse_cycle(ClusterArgs<T> P) {
+    EQC_GRID_WAIT();
     const int nthr = (int)(cluster_size() * blockDim.x);
     const int tid = (int)(cluster_rank() * blockDim.x + threadIdx.x);
 

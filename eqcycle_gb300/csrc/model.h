@@ -93,6 +93,7 @@ struct Handle {
     int64_t damage_count = 0;
     int64_t gen = 0;
     double setup_ms[5] = {0, 0, 0, 0, 0};
+    int64_t pdl_edges = 0;   // programmatic kernel-to-kernel edges in the captured graphs
     // V-cycle pointwise work fused into the operator kernels (EQC_NO_FUSE set at creation: the
     // separate kernels, for comparisons)
     bool fuse = true;   // eqc_create phases: numbering, elements, nodes, other, hierarchy
@@ -221,6 +222,11 @@ void cond_begin(Handle& h, cudaGraphConditionalNodeType type, cudaGraphCondition
 void cond_end(Handle& h);
 // Ends every capture in progress on the handle's streams and restores h.stream.
 void abort_capture(Handle& h);
+// Turns the edges of graph g between two of this library's kernels, where the second has no
+// other dependency, into programmatic edges (the second kernel's CTAs may be scheduled once
+// every CTA of the first has started; each kernel's EQC_GRID_WAIT holds them until the first
+// has finished).  Returns the number of edges changed; 0 when EQC_NO_PDL is set.
+int64_t make_programmatic(cudaGraph_t g);
 // Kernel counting during capture (count_launch adds to the capture tally instead).
 void capture_counting(bool on);
 int64_t capture_tally();

@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(NA_THREADS) k_dtevol_noalloc(const double* __r
                                                                 const double* __restrict__ XiLf, int64_t n,
                                                                 int64_t first, double dt, double dtmin, int isolver,
                                                                 DtevolScratch* S, double* out) {
+    EQC_GRID_WAIT();
     __shared__ double smin[NA_THREADS / 32];
     __shared__ bool last;
     const double dtmax = 50.0 * 24 * 60 * 60;  // src/dtevol.jl:7

@@ -43,6 +43,7 @@ __device__ __forceinline__ void material(const SetupArgs& a, int ex, int ey, int
 // One thread per element: W (FP64, FP32 and the copies padded for TMA element tiles).
 __global__ void k_setup_W(SetupArgs a, double* __restrict__ W64, float* __restrict__ W32, double* __restrict__ W64p,
                           float* __restrict__ W32p, float* __restrict__ W32lo) {
+    EQC_GRID_WAIT();
     const int64_t Nel = (int64_t)a.L.NelX * a.L.NelY;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nel; e += (int64_t)gridDim.x * blockDim.x) {
         const int ex = (int)(e % a.L.NelX), ey = (int)(e / a.L.NelX);
@@ -69,6 +70,7 @@ __global__ void k_setup_W(SetupArgs a, double* __restrict__ W64, float* __restri
 // diagonal of K (Kassemble.jl:50-58 with i = k, j = l).  Row padding: M = 1, diag = 1; the fault
 // row's diagonal is 1 (not part of the quasi-static system).
 __global__ void k_setup_nodes(SetupArgs a, double* __restrict__ M, double* __restrict__ dg64, float* __restrict__ dg32) {
+    EQC_GRID_WAIT();
     const Layout L = a.L;
     const int64_t N = L.size();
     for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
@@ -112,10 +114,12 @@ __global__ void k_setup_nodes(SetupArgs a, double* __restrict__ M, double* __res
 // M[iB] += half_dt * Bc (par.jl:173-174), the left boundary first, then the top one.
 __global__ void k_setup_boundary(double* __restrict__ M, const int64_t* __restrict__ iB, const double* __restrict__ Bc,
                                  int n, double half_dt) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x; k < n; k += blockDim.x) M[iB[k]] = M[iB[k]] + half_dt * Bc[k];
 }
 
 __global__ void k_setup_inv(const double* __restrict__ M, double* __restrict__ invM, int64_t N) {
+    EQC_GRID_WAIT();
     for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
         invM[n] = 1.0 / M[n];
 }

@@ -35,6 +35,7 @@ static_assert(offsetof(CGState, rho_prev) == 8 * S_RHOP && offsetof(CGState, pq)
 template <class T>
 __global__ void __launch_bounds__(VEC_THREADS) k_dot_rho(const T* __restrict__ x, const T* __restrict__ y, int64_t n,
                                                          double* part, unsigned* count, double* S) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     DotAcc<T> acc;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
@@ -55,6 +56,7 @@ __global__ void __launch_bounds__(VEC_THREADS) k_dot_rho(const T* __restrict__ x
 template <class T>
 __global__ void __launch_bounds__(VEC_THREADS) k_pupdate(const T* __restrict__ z, T* __restrict__ u, int64_t n,
                                                          const double* S, const int* restart) {
+    EQC_GRID_WAIT();
     const T b = *restart ? T(0) : (T)(S[S_RHO] / S[S_RHOP]);
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         T zz[4], uu[4];
@@ -71,6 +73,7 @@ template <class TX, class T>
 __global__ void __launch_bounds__(VEC_THREADS) k_xr_update(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ u,
                                                            const T* __restrict__ q, int64_t n, double* part,
                                                            unsigned* count, double* S) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     const double alpha = S[S_RHO] / S[S_PQ];
     const T a = (T)alpha;
@@ -98,6 +101,7 @@ __global__ void __launch_bounds__(VEC_THREADS) k_xr_update(TX* __restrict__ x, T
 
 template <class T>
 __global__ void k_jacobi(const T* __restrict__ r, const T* __restrict__ dg, T* __restrict__ z, int64_t n) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         z[i] = r[i] / dg[i];
 }
@@ -105,6 +109,7 @@ __global__ void k_jacobi(const T* __restrict__ r, const T* __restrict__ dg, T* _
 // x64 += (double) y32 / sigma ; y32 = 0   (sigma a power of two: the division is exact)
 __global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, float* __restrict__ y, int64_t n,
                                                       const CGState* S) {
+    EQC_GRID_WAIT();
     const double inv = 1.0 / S->sigma;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double xx[4];
@@ -121,6 +126,7 @@ __global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, fl
 // r32 = (float) (sigma r64) ; S->rr = sigma^2 r64.r64
 __global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(const double* __restrict__ r64, float* __restrict__ r32,
                                                              int64_t n, double* part, unsigned* count, CGState* S) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     const double sg = S->sigma;
     double s = 0.0;
@@ -142,6 +148,7 @@ __global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(const double* __res
 // Scale of the FP32 recurrence for this solve: sigma = 2^-e with 2^e <= ||b|| < 2^(e+1)
 // (1 in FP64, or when b = 0).
 __global__ void k_set_sigma(CGState* S, int mixed) {
+    EQC_GRID_WAIT();
     const double nb = sqrt(S->bb);
     S->sigma = (mixed && nb > 0 && isfinite(nb)) ? ldexp(1.0, -ilogb(nb)) : 1.0;
 }
@@ -154,6 +161,7 @@ static inline dim3 vgrid() { return dim3(VEC_BLOCKS); }
 
 // Start of a solve: S->bb, S->rr hold ||b||^2 and ||r0||^2.
 __global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, cudaGraphConditionalHandle hw, int use_cond) {
+    EQC_GRID_WAIT();
     const double nb = sqrt(S->bb), r = sqrt(S->rr) / S->sigma;
     const double reltol = (rule == EQC_TOL_R0 ? r : nb) * tol;
     S->nb = nb;
@@ -173,6 +181,7 @@ __global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, cudaGraph
 
 // End of an FP64 iteration: the loop goes on until ||r|| <= reltol or maxit.
 __global__ void k_cg_check(CGState* S, cudaGraphConditionalHandle hw, int use_cond) {
+    EQC_GRID_WAIT();
     S->it += 1;
     const double r = sqrt(S->rr) / S->sigma;
     S->res = r;
@@ -184,6 +193,7 @@ __global__ void k_cg_check(CGState* S, cudaGraphConditionalHandle hw, int use_co
 // Mixed precision, after the FP32 recurrences: decide whether a reliable update is due
 // (the recurrence residual fell by `delta` since the last one, or the loop would stop).
 __global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandle hi, int use_cond) {
+    EQC_GRID_WAIT();
     S->it += 1;
     S->restart = 0;   // consumed by this iteration's direction update
     const double rs = sqrt(S->rr) / S->sigma;
@@ -202,6 +212,7 @@ __global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandl
 // Mixed precision, end of the iteration: take the FP64 residual of a reliable update and
 // decide whether the loop goes on.
 __global__ void k_cg_check_b(CGState* S, Ctrl* C, cudaGraphConditionalHandle hw, int use_cond) {
+    EQC_GRID_WAIT();
     if (S->done != 3) {
         if (S->need_update) {
             const double rs = sqrt(S->rr) / S->sigma;
@@ -225,6 +236,7 @@ __global__ void k_cg_check_b(CGState* S, Ctrl* C, cudaGraphConditionalHandle hw,
 // After the loop: solve counters and failure flags in the control block.  mark_valid: the
 // loop ended on an FP64 true residual (mixed precision), which the next solve may carry.
 __global__ void k_cg_finish(const CGState* S, Ctrl* C, int mark_valid) {
+    EQC_GRID_WAIT();
     C->r_valid = (mark_valid && S->done == 1) ? 1 : 0;
     C->cg_iters += S->it;
     C->cg_solves += 1;
@@ -237,6 +249,7 @@ __global__ void k_cg_finish(const CGState* S, Ctrl* C, int mark_valid) {
 // Fault row: dF = d[k] - Flast[k] into row 0 of a work vector, Flast = d[k].
 __global__ void k_fault_delta(const double* __restrict__ d, double* __restrict__ Flast, double* __restrict__ dF,
                               int Nf) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < Nf; k += blockDim.x * gridDim.x) {
         const double f = d[k];
         dF[k] = f - Flast[k];
@@ -246,6 +259,7 @@ __global__ void k_fault_delta(const double* __restrict__ d, double* __restrict__
 
 // Carried residual, rows 1..4 (the only rows K_IF reaches): r64 += t.
 __global__ void k_carry_rows(double* __restrict__ r64, const double* __restrict__ t, int64_t n) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         r64[i] += t[i];
 }
@@ -254,6 +268,7 @@ __global__ void k_carry_rows(double* __restrict__ r64, const double* __restrict_
 // S->rr_guess = ||r32||^2 (S->rr keeps the residual without the increment).
 __global__ void __launch_bounds__(VEC_THREADS) k_guess_residual(float* __restrict__ r32, const float* __restrict__ t,
                                                                 int64_t n, double* part, unsigned* count, CGState* S) {
+    EQC_GRID_WAIT();
     __shared__ double sh[32];
     const float sg = (float)S->sigma;
     DotAcc<float> acc;
@@ -274,6 +289,7 @@ __global__ void __launch_bounds__(VEC_THREADS) k_guess_residual(float* __restric
 
 // The previous-step guess judges the increment: keep it only if it lowered ||r||.
 __global__ void k_guess_decide(CGState* S, Ctrl* C) {
+    EQC_GRID_WAIT();
     const int keep = S->rr_guess < S->rr ? 1 : 0;
     S->guess_keep = keep;
     if (keep) S->rr = S->rr_guess;
@@ -284,6 +300,7 @@ __global__ void k_guess_decide(CGState* S, Ctrl* C) {
 __global__ void __launch_bounds__(VEC_THREADS) k_guess_revert(const CGState* S, double* __restrict__ d,
                                                               const float* __restrict__ g, float* __restrict__ r32,
                                                               const double* __restrict__ r64, int64_t n) {
+    EQC_GRID_WAIT();
     if (S->guess_keep) return;
     const double sg = S->sigma;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -294,6 +311,7 @@ __global__ void __launch_bounds__(VEC_THREADS) k_guess_revert(const CGState* S, 
 
 // Chooses the residual set-up of a solve: carry (r_valid) or a full FP64 apply.
 __global__ void k_setup_select(Ctrl* C, cudaGraphConditionalHandle hc, cudaGraphConditionalHandle hf, int use_cond) {
+    EQC_GRID_WAIT();
     const unsigned v = C->r_valid ? 1u : 0u;
     C->cg_carried += v;
     if (use_cond) {

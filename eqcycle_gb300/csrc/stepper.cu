@@ -27,6 +27,7 @@ static inline int fblocks(int Nf) { return (Nf + FNT - 1) / FNT; }
 // Vf0 = 2 v[iFlt] + Vpl ; Vf = Vf0 ; d[iFlt] = F = dPre[iFlt] + v[iFlt] dt  (main.jl:231-238)
 __global__ void __launch_bounds__(FNT) k_qs_begin(double* __restrict__ d, const double* __restrict__ dPre, const double* __restrict__ v,
                            double* Vf0, double* Vf, int Nf, const Ctrl* C) {
+    EQC_GRID_WAIT();
     const double dt = C->dt, Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < Nf; k += blockDim.x * gridDim.x) {
         const double a = 2 * v[k] + Vpl;
@@ -41,6 +42,7 @@ __global__ void __launch_bounds__(FNT) k_qs_begin(double* __restrict__ d, const 
 // g = (dt / dt_prev) (d - dPre_old) (g also kept in FP32 for the residual correction).
 __global__ void k_qs_begin_bulk(double* __restrict__ d, double* __restrict__ dPre, float* __restrict__ g, int64_t n,
                                 int64_t ld, int extrap, const Ctrl* C) {
+    EQC_GRID_WAIT();
     const bool use = extrap && C->qs_prev && C->dt_prev > 0;
     const double ratio = use ? C->dt / C->dt_prev : 0.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -69,6 +71,7 @@ struct FaultArgs {
 
 __global__ void __launch_bounds__(FNT) k_qs_fault(const double* __restrict__ Kd0, double* __restrict__ v, double* __restrict__ d,
                            const double* __restrict__ dPre, FaultArgs f, const Ctrl* C, int next_F) {
+    EQC_GRID_WAIT();
     const double dt = C->dt, Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         const double ak = f.bcflag[k] ? 0. : Kd0[k];
@@ -90,6 +93,7 @@ __global__ void __launch_bounds__(FNT) k_qs_fault(const double* __restrict__ Kd0
 
 // End of the quasi-static step on the fault (main.jl:283-288).
 __global__ void __launch_bounds__(FNT) k_qs_end_fault(double* __restrict__ v, FaultArgs f, const Ctrl* C) {
+    EQC_GRID_WAIT();
     const double Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         f.psi[k] = f.psi1[k];
@@ -106,6 +110,7 @@ __global__ void __launch_bounds__(FNT) k_qs_end_fault(double* __restrict__ v, Fa
 // v[FltNI] = (d - dPre)/dt ; a = 0  (main.jl:289-292), rows >= 1
 __global__ void k_qs_end_bulk(const double* __restrict__ d, const double* __restrict__ dPre, double* __restrict__ v,
                               double* __restrict__ a, int64_t ld, int64_t n, Ctrl* C) {
+    EQC_GRID_WAIT();
     const double dt = C->dt;
     if (blockIdx.x == 0 && threadIdx.x == 0) C->kd_valid = 0;   // d changed: no incremental K d
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -116,6 +121,7 @@ __global__ void k_qs_end_bulk(const double* __restrict__ d, const double* __rest
 
 // x[list] = 0 for up to three arrays
 __global__ void k_zero_list(const int64_t* __restrict__ idx, int n, double* x, double* y, double* z) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < n; k += blockDim.x * gridDim.x) {
         const int64_t g = idx[k];
         if (x) x[g] = 0.;
@@ -128,6 +134,7 @@ __global__ void k_zero_list(const int64_t* __restrict__ idx, int n, double* x, d
 // vPre on the fault; d += dt v + dt^2/2 a ; v += dt/2 a   (main.jl:299-306)
 __global__ void k_dyn_predict(double* __restrict__ d, double* __restrict__ v, const double* __restrict__ a,
                               double* __restrict__ vPre_f, int Nf, int64_t n, Ctrl* C) {
+    EQC_GRID_WAIT();
     const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // d changes: no carried residual, no QS history
         C->r_valid = 0;
@@ -152,6 +159,7 @@ __global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d,
                                                          float* __restrict__ dd32, int Nf, int64_t n, Ctrl* C,
                                                          cudaGraphConditionalHandle hf, cudaGraphConditionalHandle hi,
                                                          int use_cond) {
+    EQC_GRID_WAIT();
     const double dt = C->dt, hdt = C->half_dt, hdt2 = C->half_dt_sq;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         C->r_valid = 0;
@@ -187,6 +195,7 @@ __global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d,
 // a = -K d with K d either refreshed (Kd written by the FP64 apply) or Kd += K dd (t32, FP32).
 __global__ void __launch_bounds__(256) k_dyn_force(double* __restrict__ Kd, const float* __restrict__ t32,
                                                    double* __restrict__ a, int64_t n, Ctrl* C) {
+    EQC_GRID_WAIT();
     const int full = C->kd_full;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double k[4];
@@ -211,6 +220,7 @@ __global__ void __launch_bounds__(256) k_dyn_force(double* __restrict__ Kd, cons
 // a[FltIglobBC] = 0 ; absorbing boundaries (main.jl:314-318), one CTA, L then T.
 __global__ void k_dyn_bc(double* __restrict__ a, const double* __restrict__ v, const int64_t* iBC, int nBC,
                          const int64_t* iL, const double* CL, int nL, const int64_t* iT, const double* CT, int nT) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x; k < nBC; k += blockDim.x) a[iBC[k]] = 0.;
     __syncthreads();
     for (int k = threadIdx.x; k < nL; k += blockDim.x) a[iL[k]] = a[iL[k]] - CL[k] * v[iL[k]];
@@ -223,6 +233,7 @@ __global__ void k_dyn_bc(double* __restrict__ a, const double* __restrict__ v, c
 __global__ void k_dyn_bc_nodes(double* __restrict__ a, const double* __restrict__ v, const int64_t* __restrict__ node,
                                const int* __restrict__ ops, const double* __restrict__ cl, const double* __restrict__ ct,
                                int n) {
+    EQC_GRID_WAIT();
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += blockDim.x * gridDim.x) {
         const int64_t i = node[k];
         const int op = ops[k];
@@ -237,6 +248,7 @@ __global__ void k_dyn_bc_nodes(double* __restrict__ a, const double* __restrict_
 // Fault boundary condition (main.jl:321-331): FltVfree, Vf, FBC! (two NR solves per node),
 // tau = tau2 - tauo, psi = psi2, a[iFlt] -= FltB tau.
 __global__ void __launch_bounds__(FNT) k_dyn_fault(double* __restrict__ a, const double* __restrict__ v, FaultArgs f, Ctrl* C) {
+    EQC_GRID_WAIT();
     const double dt = C->dt, hdt = C->half_dt, Vpl = C->Vpl;
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         const double vfree = 2 * v[k] + 2 * hdt * a[k] / f.Mf[k];
@@ -270,6 +282,7 @@ __global__ void __launch_bounds__(FNT) k_dyn_fault(double* __restrict__ a, const
 // instead of GB300's slow FP64 division; the plain method divides as the reference does).
 __global__ void k_dyn_correct(double* __restrict__ a, double* __restrict__ v, const double* __restrict__ M, int64_t n,
                               const Ctrl* C, int inv) {
+    EQC_GRID_WAIT();
     const double hdt = C->half_dt;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double ai = inv ? a[i] * M[i] : a[i] / M[i];
@@ -282,6 +295,7 @@ __global__ void k_dyn_correct(double* __restrict__ a, double* __restrict__ v, co
 __global__ void __launch_bounds__(256) k_dyn_correct_inv(double* __restrict__ a, double* __restrict__ v,
                                                          const double* __restrict__ invM, int64_t n, const Ctrl* C,
                                                          int64_t nzero) {
+    EQC_GRID_WAIT();
     const double hdt = C->half_dt;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double aa[4], vv[4], mm[4];
@@ -303,6 +317,7 @@ __global__ void __launch_bounds__(256) k_dyn_correct_inv(double* __restrict__ a,
 // Vfmax (main.jl:348), hypocentre argmax (main.jl:367), regime switch (main.jl:439-443),
 // next dt (dtevol!, src/dtevol.jl:5-44).  One CTA.
 __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, FaultArgs f, Ctrl* C) {
+    EQC_GRID_WAIT();
     __shared__ double smax[FT / 32];
     __shared__ int sidx[FT / 32];
     __shared__ double smin[FT / 32];
@@ -369,6 +384,7 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
 // Gather d, v, a at receivers (main.jl:433-435) into out[3*ns].
 __global__ void k_gather_seis(const int64_t* idx, int ns, const double* d, const double* v, const double* a,
                               double* out) {
+    EQC_GRID_WAIT();
     const int k = threadIdx.x;
     if (k < ns) {
         out[k] = d[idx[k]];
@@ -400,6 +416,7 @@ static void launch_check() { EQC_CHECK_LAUNCH(); }
 
 // --- fault-only API helpers (eqc_slrFunc / eqc_FBC / eqc_dtevol) ---------------------------
 __global__ void __launch_bounds__(FNT) k_api_slr(FaultArgs f, double dt) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         if (k < f.NFBC0) continue;
         const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, f.Vf[k], 1e-6);
@@ -408,6 +425,7 @@ __global__ void __launch_bounds__(FNT) k_api_slr(FaultArgs f, double dt) {
     }
 }
 __global__ void __launch_bounds__(FNT) k_api_fbc(FaultArgs f, double dt, int* fail) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
         if (k < f.NFBC0) continue;
         const double vf = f.Vf[k], vfree = f.FltVfree[k];
@@ -477,6 +495,7 @@ int fault_FBC(Handle& h, double* psi1, double* Vf1, double* tau1, double* psi2, 
 }
 
 __global__ void k_api_dtevol(const double* Vf, FaultArgs f, double dt, double dtmin, int isolver, double* out) {
+    EQC_GRID_WAIT();
     __shared__ double smin[FT / 32];
     const double dtmax = 50.0 * 24 * 60 * 60;
     double dmin = dtmax;
@@ -520,21 +539,25 @@ double fault_dtevol(Handle& h, double dt, double dtmin, const double* Vf, int is
 
 // --- state initialisation (main.jl:89-190) -----------------------------------------------
 __global__ void __launch_bounds__(FNT) k_init_psi(const double* v, FaultArgs f) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x)
         f.psi[k] = f.tauo[k] / (f.Seff[k] * f.ccb[k]) - f.fo[k] / f.ccb[k] -
                    (f.cca[k] / f.ccb[k]) * log(2 * v[k] / f.Vo[k]);
 }
 __global__ void k_fill(double* x, double val, int64_t n) {
+    EQC_GRID_WAIT();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = val;
 }
 // Fill value only on real nodes (row padding stays zero).
 __global__ void k_fill_nodes(double* x, double val, Layout L) {
+    EQC_GRID_WAIT();
     const int64_t n = L.size();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = ((i % L.ld) < L.nx) ? val : 0.0;
 }
 __global__ void __launch_bounds__(FNT) k_init_Vf(const double* v, FaultArgs f) {
+    EQC_GRID_WAIT();
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x)
         f.Vf[k] = f.creep[k] ? 0. : 2 * v[k];
 }
@@ -599,6 +622,7 @@ static void fault_columns(Handle& h, std::vector<double>& dF, std::vector<double
 
 // it = it + 1 ; t = t + dt  (main.jl:221-222), dt of this step = C->dt
 __global__ void k_step_begin(Ctrl* C) {
+    EQC_GRID_WAIT();
     C->it += 1;
     C->t = C->t + C->dt;
 }
@@ -734,6 +758,7 @@ __global__ void k_step_end(Ctrl* C, double* __restrict__ log_t, double* __restri
                            double* __restrict__ log_seis, const int64_t* __restrict__ iSeis, int ns,
                            const double* __restrict__ d, const double* __restrict__ v, const double* __restrict__ a,
                            int regime, cudaGraphConditionalHandle hw) {
+    EQC_GRID_WAIT();
     __shared__ int rec;
     const long long it = C->it;
     const int k = C->nlog;
@@ -790,6 +815,7 @@ static StepGraph& batched_graph(Handle& h, int iso) {
         count_launch();
         cond_end(h);
         EQC_CUDA(cudaStreamEndCapture(h.stream, &G.graph));
+        h.pdl_edges += make_programmatic(G.graph);
     } catch (...) {
         abort_capture(h);
         h.capturing = nullptr;
@@ -813,6 +839,7 @@ static StepGraph& step_graph(Handle& h, int iso) {
         EQC_CUDA(cudaStreamBeginCapture(h.stream, cudaStreamCaptureModeThreadLocal));
         enqueue_step(h, iso, true);
         EQC_CUDA(cudaStreamEndCapture(h.stream, &G.graph));
+        h.pdl_edges += make_programmatic(G.graph);
     } catch (...) {
         abort_capture(h);
         h.capturing = nullptr;

@@ -8,6 +8,7 @@ namespace eqc {
 // timed kernel pays no write-back of someone else's dirty data (a read-modify-write flush
 // would leave L2 full of dirty lines and inflate the next kernel's DRAM traffic).
 __global__ void k_flush(const float4* __restrict__ buf, int64_t n4, float* sink) {
+    EQC_GRID_WAIT();
     float s = 0.f;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
         const float4 v = buf[i];

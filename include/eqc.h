@@ -257,7 +257,9 @@ eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
  * the solver settings "apply_variant" and "reliable_delta" (as chosen by eqc_autotune), and
  * "damage_events" (damage steps applied, eqc_set_damage), and the host time in ms of the
  * phases of eqc_create: "setup_ms_numbering", "setup_ms_elements", "setup_ms_nodes",
- * "setup_ms_other", "setup_ms_hierarchy" (the multigrid hierarchy)).
+ * "setup_ms_other", "setup_ms_hierarchy" (the multigrid hierarchy), and "pdl_edges", the
+ * kernel-to-kernel edges of the captured step graphs launched as programmatic dependent
+ * launches (0 with the environment variable EQC_NO_PDL set at capture)).
  * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);

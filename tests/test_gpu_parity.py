@@ -169,7 +169,9 @@ def test_multigrid_time_loop_matches_oracle(eqclib, oracle_mod):
 def test_graph_step_equals_eager_step(eqclib, precision, guess):
     """A step replayed from its CUDA graph (device-driven CG loop in conditional nodes) runs
     the same kernels in the same order as the host-driven step: bitwise equal state and the
-    same iteration counts, through quasi-static and dynamic steps."""
+    same iteration counts, through quasi-static and dynamic steps.  The graphs launch
+    consecutive kernels as programmatic dependent launches (pdl_edges > 0); the eager steps do
+    not, so equality also shows that every kernel waits for its predecessor."""
     cfg = preset("dz40").replace(V_init=2e-2)
     P = set_parameters(cfg)
     out = []
@@ -178,6 +180,8 @@ def test_graph_step_equals_eager_step(eqclib, precision, guess):
             s.init(cfg.V_init)
             st = s.run(12)
             out.append((st, {k: s.state(k) for k in ("d", "v", "a", "psi", "tau")}))
+            pdl = s.scalar("pdl_edges")
+            assert (pdl > 0) if graphs else (pdl == 0)
     (st0, x0), (st1, x1) = out
     assert st0["qs_steps"] >= 1 and st0["dyn_steps"] >= 1, st0
     for k in ("steps", "qs_steps", "dyn_steps", "cg_iters", "qs_solves", "isolver"):
