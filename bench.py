@@ -554,15 +554,22 @@ def bench_learned(args):
 def bench_ensemble(args):
     """The batched ensemble: 64 uneven damage-zone models (120x60 to 480x240 elements, seeded
     parameters) advanced by one CUDA-graph launch per step, mixed precision with the extrapolated
-    guess; compared with the same members stepped one after another with their own graphs."""
+    guess; compared with the same members stepped one after another with their own graphs.  Under
+    torchrun the members are split across the ranks (shard_members; no exchange), each rank runs
+    its share as one ensemble, and the whole-job value is all ranks' simulated years over the
+    slowest rank's device time (a fixed total of members: strong scaling)."""
     from eqcycle_gb300 import (EQC_GUESS_EXTRAPOLATE, EQC_MIXED, Ensemble, Solver, ensemble_members,
                                structured_parameters)
+    from eqcycle_gb300.config import shard_members
+    rank, ws, dist = _dist()
+    device = int(os.environ.get("LOCAL_RANK", "0"))
     t0 = time.time()
-    cfgs = ensemble_members(args.members)
+    cfgs_all = ensemble_members(args.members)
+    cfgs = [cfgs_all[k] for k in shard_members(cfgs_all, rank, ws)]
     solvers, nodes = [], 0
     for c in cfgs:
         P = structured_parameters(c)   # element and node data built on the device
-        s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, guess=EQC_GUESS_EXTRAPOLATE)
+        s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device, guess=EQC_GUESS_EXTRAPOLATE)
         s.init(c.V_init)
         s.set_scalar("dt", steady_dt(s, P))
         solvers.append(s)
@@ -571,21 +578,27 @@ def bench_ensemble(args):
     E = Ensemble(solvers)
     E.run(args.warmup)
     t_start = [s.scalar("t") for s in solvers]
+    _barrier(dist)
     stats, ms = E.run(args.steps)
-    years = sum((st["t"] - t0_) / YR for st, t0_ in zip(stats, t_start))
-    value = years / (ms / 3.6e6)
+    _barrier(dist)
+    ms_max = _allreduce(dist, ms, _max_op())
+    years = _allreduce(dist, sum((st["t"] - t0_) / YR for st, t0_ in zip(stats, t_start)), _sum_op())
+    value = years / (ms_max / 3.6e6)
     # the same number of steps, member after member (each with its own step graph)
     t_seq = [s.scalar("t") for s in solvers]
     seq_ms = 0.0
     for s in solvers:
         seq_ms += s.run(args.steps)["gpu_ms"]
-    seq_years = sum((s.scalar("t") - t) / YR for s, t in zip(solvers, t_seq))
-    line = {"metric": "ensemble sim-years/hr", "value": value, "unit": "sim-years/hr", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(args.steps, 1),
-            "higher_is_better": True, "members": len(solvers), "nodes_total": nodes,
-            "qs_steps": int(sum(st["qs_steps"] for st in stats)), "dyn_steps": int(sum(st["dyn_steps"] for st in stats)),
-            "cg_iters_per_solve": sum(st["cg_iters"] for st in stats) / max(1, sum(st["qs_solves"] for st in stats)),
-            "sequential": {"value": seq_years / (seq_ms / 3.6e6), "ms_per_step": seq_ms / max(args.steps, 1)},
+    seq_ms_max = _allreduce(dist, seq_ms, _max_op())
+    seq_years = _allreduce(dist, sum((s.scalar("t") - t) / YR for s, t in zip(solvers, t_seq)), _sum_op())
+    cnt = lambda key: int(_allreduce(dist, sum(st[key] for st in stats), _sum_op()))
+    qs, dyn, cg, solves = cnt("qs_steps"), cnt("dyn_steps"), cnt("cg_iters"), cnt("qs_solves")
+    line = {"metric": "ensemble sim-years/hr", "value": value, "unit": "sim-years/hr", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "strong", "members": len(cfgs_all),
+            "members_rank0": len(solvers), "nodes_total": int(_allreduce(dist, nodes, _sum_op())),
+            "qs_steps": qs, "dyn_steps": dyn, "cg_iters_per_solve": cg / max(1, solves),
+            "sequential": {"value": seq_years / (seq_ms_max / 3.6e6), "ms_per_step": seq_ms_max / max(args.steps, 1)},
             "setup_s": setup_s,
             "config": {"workload": f"{len(solvers)} damage-zone models, 120x60 to 480x240 elements, seeded "
                                    f"parameters; one graph launch per ensemble step; mixed precision, "
@@ -593,7 +606,8 @@ def bench_ensemble(args):
     E.close()
     for s in solvers:
         s.close()
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def bench_cycle(args):

@@ -149,3 +149,20 @@ def ensemble_members(n: int = 64, seed: int = 0, nmin: int = 120, nmax: int = 48
             trap_w0=w, trap_w1=0.4 * w, vs2=(1.0 - red) * 3464.0, Dc=Dc, b0=0.015 - amb, total_years=500.0)
         out.append(cfg)
     return out
+
+
+def shard_members(cfgs, rank: int, world: int):
+    """Indices (ascending) of the ensemble members that rank ``rank`` of ``world`` runs.  The
+    members are independent models, so they split across GPUs with no exchange: largest first,
+    each to the rank with the fewest nodes so far (ties to the lower rank); every member lands on
+    exactly one rank and the node counts of the ranks differ by at most one member's."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside a world of {world}")
+    nodes = [(4 * c.NelX + 1) * (4 * c.NelY + 1) for c in cfgs]
+    load = [0] * world
+    own = [[] for _ in range(world)]
+    for k in sorted(range(len(cfgs)), key=lambda k: (-nodes[k], k)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        load[r] += nodes[k]
+        own[r].append(k)
+    return sorted(own[rank])
