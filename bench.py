@@ -145,24 +145,32 @@ class Clocks:
         except Exception:
             self.p.kill()
         self.f.close()
-        sm, smax, reasons = [], 0.0, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax = max(smax, float(parts[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, parts[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(n)
-        if not sm:
-            return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm), "source": "nvidia-smi, 200 ms"}
+        with open(self.path) as f:
+            return parse_clock_csv(f)
+
+
+def parse_clock_csv(lines):
+    """Clock record from nvidia-smi's CSV lines (the query of Clocks, noheader, nounits): median SM
+    clock, maximum SM clock, and the throttle reasons seen active in any sample; None without a
+    valid sample.  Lines that do not parse (a partial last line, "[N/A]") are skipped."""
+    sm, smax, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in lines:
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9:
+            continue
+        try:
+            sm.append(float(parts[1]))
+            smax = max(smax, float(parts[2]))
+        except ValueError:
+            continue
+        for n, v in zip(names, parts[5:9]):
+            if v.lower().startswith("active"):
+                reasons.add(n)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+            "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 def steady_dt(solver, P):
