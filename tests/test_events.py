@@ -4,7 +4,6 @@ import os
 from dataclasses import fields
 
 import numpy as np
-import pytest
 
 from eqcycle_gb300.events import catalogue, compare, load_results, moment_magnitude, save_results
 from eqcycle_gb300.solver import Results
