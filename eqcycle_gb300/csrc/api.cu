@@ -385,12 +385,24 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     h.setup_ms[4] = ms_since(t0);   // multigrid hierarchy (host Galerkin products, device bounds)
 }
 
+// Reference numbering <-> node layout on the host's cores: ref2lay is one-to-one, so the
+// chunks write disjoint entries (the layout's row padding stays zero).
 static void to_layout(const Handle& h, const double* ref, std::vector<double>& lay) {
-    lay.assign(h.L.size(), 0.0);
-    for (int64_t g = 0; g < h.nglob; ++g) lay[h.ref2lay[g]] = ref[g];
+    constexpr int64_t CH = 1 << 16;
+    const int64_t N = h.L.size();
+    lay.resize(N);
+    parallel_for((N + CH - 1) / CH, [&](int64_t c) {
+        std::fill(lay.begin() + c * CH, lay.begin() + std::min(N, (c + 1) * CH), 0.0);
+    });
+    parallel_for((h.nglob + CH - 1) / CH, [&](int64_t c) {
+        for (int64_t g = c * CH; g < std::min(h.nglob, (c + 1) * CH); ++g) lay[h.ref2lay[g]] = ref[g];
+    });
 }
 static void from_layout(const Handle& h, const std::vector<double>& lay, double* ref) {
-    for (int64_t g = 0; g < h.nglob; ++g) ref[g] = lay[h.ref2lay[g]];
+    constexpr int64_t CH = 1 << 16;
+    parallel_for((h.nglob + CH - 1) / CH, [&](int64_t c) {
+        for (int64_t g = c * CH; g < std::min(h.nglob, (c + 1) * CH); ++g) ref[g] = lay[h.ref2lay[g]];
+    });
 }
 
 static thread_local std::string g_create_err;
