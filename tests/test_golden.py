@@ -72,3 +72,26 @@ def test_event_catalogue_fixture_is_consistent(gold):
     assert len(tS) >= 2 and len(tE) == len(tS)
     assert np.all(tE > tS) and np.all(np.diff(tS) > 0) and tE[-1] <= years * YR2SEC
     assert np.all(gold["ev_max_slip"] > 0) and np.all(np.isfinite(gold["ev_Mw"]))
+
+
+NUCL = os.path.join(os.path.dirname(__file__), "golden", "nucleation_homog48.npz")
+
+
+def test_nucleation_history_fixture(oracle_mod):
+    """The oracle's homog48 history through the first nucleation (make_nucleation_golden.py):
+    consistent on its own, and its first 10 steps reproduced by running the oracle again (the
+    whole history takes the oracle most of an hour)."""
+    from eqcycle_gb300.config import preset
+    g = dict(np.load(NUCL))
+    nsteps, check, tol = int(g["info"][0]), int(g["info"][1]), float(g["info"][2])
+    assert len(g["time"]) == len(g["Vfmax"]) == len(g["regime"]) == nsteps
+    cfg = preset("homog48")
+    assert g["Vfmax"][-1] > 1.01 * cfg.Vthres and np.all(g["Vfmax"][:-1] <= 1.01 * cfg.Vthres)
+    assert np.all(g["regime"] == 1)                      # the nucleation is quasi-static throughout
+    assert np.all(np.diff(g["time"]) > 0) and g["check_steps"][-1] == nsteps
+    assert list(g["check_steps"][:-1]) == list(range(check, nsteps, check))[:len(g["check_steps"]) - 1]
+    assert g["d_fault"].shape == g["v_fault"].shape == g["psi"].shape == (len(g["check_steps"]), 193)
+    o = oracle_mod.Oracle(cfg)
+    assert o.run(10, qs_mode=0, qs_tol=tol) == 10
+    assert rel(o.get("time_"), g["time"][:10]) <= 1e-12
+    assert rel(o.get("Vfmax"), g["Vfmax"][:10]) <= 1e-10
