@@ -53,7 +53,7 @@ class EqcOptions(C.Structure):
                 ("cg_tol", C.c_double), ("cg_maxit", C.c_int32), ("device", C.c_int32),
                 ("use_graphs", C.c_int32), ("verbose", C.c_int32),
                 ("reliable_delta", C.c_double), ("mg_degree", C.c_int32), ("mg_coarse_max", C.c_int32),
-                ("mg_cluster_max", C.c_int32), ("apply_variant", C.c_int32), ("mg_degree_coarse", C.c_int32),
+                ("apply_variant", C.c_int32), ("mg_degree_coarse", C.c_int32),
                 ("step_batch", C.c_int32)]
 
 

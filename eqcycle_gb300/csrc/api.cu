@@ -504,6 +504,7 @@ eqc_status eqc_apply_K(eqc_handle* H, const double* x, double* y) {
         apply_K<double>(h.tmp64a.p, h.tmp64b.p, args64(h), 1.0, 0, h.stream);
         h.tmp64b.download(yl.data(), yl.size(), h.stream);
         EQC_CUDA(cudaStreamSynchronize(h.stream));
+        check_apply_err(h);
         from_layout(h, yl, y);
     });
 }
@@ -627,6 +628,8 @@ eqc_status eqc_get_scalar(eqc_handle* H, const char* name, double* out) {
         else if (s == "setup_ms_other") *out = h.setup_ms[3];
         else if (s == "setup_ms_hierarchy") *out = h.setup_ms[4];
         else if (s == "pdl_edges") *out = (double)h.pdl_edges;
+        else if (s == "tma_wait_polls") *out = h.tma_wait_polls;
+        else if (s == "time_capacity") *out = (double)h.cap_time;
         else if (s == "reliable_delta") *out = h.opt.reliable_delta > 0 ? h.opt.reliable_delta : 1e-3;
         else if (s == "dt") *out = C.dt;
         else if (s == "isolver") *out = C.isolver;
@@ -649,8 +652,21 @@ eqc_status eqc_set_scalar(eqc_handle* H, const char* name, double value) {
     if (!H || !name) return EQC_E_ARG;
     return guarded(H, [&] {
         Handle& h = H->h;
-        if (!h.initialized) throw Error(EQC_E_STATE, "eqc_set_scalar before eqc_init");
         const std::string s(name);
+        if (s == "tma_wait_polls") {   // bound of the TMA applies' first tile wait (failure tests)
+            if (!(value >= 0 && value <= MBAR_SPIN_LIMIT) || value != (double)(int)value)
+                throw Error(EQC_E_ARG, "tma_wait_polls must be an integer in [0, " + std::to_string(MBAR_SPIN_LIMIT) + "]");
+            h.tma_wait_polls = (int)value;
+            destroy_graphs(h);   // captured launches hold the old bound
+            return;
+        }
+        if (s == "time_capacity") {    // length of the time_ / Vfmax records (main.jl:154-163)
+            if (!(value >= 1 && value <= 1900000) || value != (double)(int64_t)value)
+                throw Error(EQC_E_ARG, "time_capacity must be an integer in [1, 1900000]");
+            h.cap_time = (int64_t)value;
+            return;
+        }
+        if (!h.initialized) throw Error(EQC_E_STATE, "eqc_set_scalar before eqc_init");
         Ctrl& C = *h.h_ctrl;
         if (s == "t") C.t = value;
         else if (s == "dt") {

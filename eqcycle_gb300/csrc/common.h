@@ -122,7 +122,13 @@ struct ApplyArgs {
     int* err;         // device flag set when a bounded wait gives up (may be null)
     TmaCache* tma;    // host-side tensor-map cache (may be null)
     int variant;      // see eqc_options.apply_variant
+    int wait_polls;   // poll bound of a TMA kernel's first tile wait (the later waits and the
+                      // drain after a give-up keep MBAR_SPIN_LIMIT); lowered only to test the
+                      // give-up path (eqc_set_scalar "tma_wait_polls")
 };
+
+// Bound, in polls of mbarrier.try_wait, of every wait of the TMA-fed stiffness applies.
+constexpr int MBAR_SPIN_LIMIT = 1 << 22;
 
 // Error text for entry points without a handle (returned by eqc_last_error(NULL)).
 void set_thread_error(const std::string& msg);

@@ -346,7 +346,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
 }
 
 constexpr int UPT = 40;                    // node-tile row pitch of the TMA box (16-byte multiple)
-constexpr int MBAR_SPIN_LIMIT = 1 << 22;   // bounded wait on the TMA barrier
 
 // Full apply with the node tile and the element tile fetched by TMA.  The node box starts at
 // x = 4*ex0 - 4 (a multiple of 4 elements, hence 16-byte aligned) and the hardware fills
@@ -379,12 +378,15 @@ __global__ void __launch_bounds__(NT) k_apply_tma(const __grid_constant__ CUtens
         tma_load_2d(ws, &wmap, &bar, (ex0 - 1) * WP, ey0 - 1);
     }
     bool done = false;
-    for (int it = 0; it < MBAR_SPIN_LIMIT && !done; ++it) done = mbar_try_wait(&bar, 0);
-    if (!done) {
-        // give up: flag it, wait (bounded) for the copies still targeting this CTA, leave
-        if (threadIdx.x == 0 && A.err) atomicExch(A.err, 1);
-        for (int it = 0; it < MBAR_SPIN_LIMIT; ++it)
-            if (mbar_try_wait(&bar, 0)) break;
+    for (int it = 0; it < A.wait_polls && !done; ++it) done = mbar_try_wait(&bar, 0);
+    if (__syncthreads_or(!done)) {
+        // give up (every thread of the CTA alike): flag it, wait (bounded) for the copies still
+        // targeting this CTA, leave
+        if (threadIdx.x == 0) {
+            if (A.err) atomicExch(A.err, 1);
+            for (int it = 0; it < MBAR_SPIN_LIMIT; ++it)
+                if (mbar_try_wait(&bar, 0)) break;
+        }
         return;
     }
     lines_compute<T, TEX, TEY, NT, UPT, WP>(us, ws, ys, cx, cy, y, A, ex0, ey0, sign, zero_row0);
@@ -441,7 +443,8 @@ __global__ void __launch_bounds__(NT) k_apply_pipe(const __grid_constant__ CUten
         const int st = i % PSTAGES;
         const uint32_t parity = (uint32_t)((i / PSTAGES) & 1);
         bool done = false;
-        for (int it = 0; it < MBAR_SPIN_LIMIT && !done; ++it) done = mbar_try_wait(&bar[st], parity);
+        const int polls = i == 0 ? A.wait_polls : MBAR_SPIN_LIMIT;
+        for (int it = 0; it < polls && !done; ++it) done = mbar_try_wait(&bar[st], parity);
         if (__syncthreads_or(!done)) {
             // give up: flag it, wait (bounded) for every copy still targeting this CTA, leave
             if (threadIdx.x == 0) {
@@ -755,7 +758,8 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
         const int st = k & 1;
         const uint32_t parity = (uint32_t)((k >> 1) & 1);
         bool done = false;
-        for (int it = 0; it < MBAR_SPIN_LIMIT && !done; ++it) done = mbar_try_wait(&bar[st], parity);
+        const int polls = k == 0 ? A.wait_polls : MBAR_SPIN_LIMIT;
+        for (int it = 0; it < polls && !done; ++it) done = mbar_try_wait(&bar[st], parity);
         if (__syncthreads_or(!done)) {
             // give up: flag it, wait (bounded) for the copies still in flight (tile 0, or tiles
             // k and k + 1), leave

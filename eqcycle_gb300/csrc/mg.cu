@@ -248,7 +248,6 @@ template <> struct Sel<double> {
     static const double* rwx(DevTransfer& t) { return t.rwx64.p; }
     static const double* rwy(DevTransfer& t) { return t.rwy64.p; }
     static ApplyArgs<double> args(Handle& h) { return args64(h); }
-    static ClusterArgs<double>& cargs(MGHier& m) { return m.ca64; }
 };
 template <> struct Sel<float> {
     static float* x(MGWork& w) { return w.x32.p; }
@@ -265,7 +264,6 @@ template <> struct Sel<float> {
     static const float* rwx(DevTransfer& t) { return t.rwx32.p; }
     static const float* rwy(DevTransfer& t) { return t.rwy32.p; }
     static ApplyArgs<float> args(Handle& h) { return args32(h); }
-    static ClusterArgs<float>& cargs(MGHier& m) { return m.ca32; }
 };
 
 template <class T>
@@ -378,10 +376,6 @@ template <class T>
 static void vcycle(Handle& h, int l, T* x, const T* b, bool first_done = false) {
     MGHier& m = *h.mg;
     const int L = (int)m.lev.size();
-    if (l == m.cl_first && m.cl_size > 0) {   // the rest of the cycle in one cluster launch
-        cluster_cycle<T>(Sel<T>::cargs(m), m.cl_size, h.stream);
-        return;
-    }
     if (l == L) {  // coarsest: dense solve on rows >= 1
         StencilLevel& c = m.lev[L - 1];
         const int64_t n = (int64_t)c.cx * c.cy;
@@ -412,10 +406,9 @@ static void vcycle(Handle& h, int l, T* x, const T* b, bool first_done = false) 
     T* bc = Sel<T>::b(wc);
     T* xc = Sel<T>::x(wc);
     const GllW<T> gw = gll_weights<T>(m);
-    // the coarse level's first smoothing step rides on the restriction (not into the dense level
-    // or a cluster-resident cycle)
+    // the coarse level's first smoothing step rides on the restriction (not into the dense level)
     ChebFirst<T> F;
-    const bool fuse = h.fuse && l + 1 < L && !(l + 1 == m.cl_first && m.cl_size > 0);
+    const bool fuse = h.fuse && l + 1 < L;
     if (fuse) {
         F.dinv = Sel<T>::Di(m.lev[l]);
         F.x = xc;
@@ -523,67 +516,6 @@ static double estimate_lmax(Handle& h, int l) {
     return 1.1 * lam;
 }
 
-// Arguments of the cluster-resident coarse cycle: every level (work indexing) from the first
-// with at most cluster_max unknowns down to the dense coarsest level.
-template <class T>
-static void setup_cluster_cycle(Handle& h) {
-    MGHier& m = *h.mg;
-    ClusterArgs<T>& P = Sel<T>::cargs(m);
-    P = ClusterArgs<T>{};
-    const int L = (int)m.lev.size();
-    const int64_t cl_max = h.opt.mg_cluster_max == 0 ? -1 : h.opt.mg_cluster_max;   // off unless asked for
-    int first = -1;
-    for (int l = 1; l <= L; ++l)
-        if ((int64_t)m.lev[l - 1].cx * m.lev[l - 1].cy <= cl_max) { first = l; break; }
-    if (cl_max < 0 || first < 0 || L - first > CL_MAXLEV || m.deg_coarse > CL_MAXDEG) {
-        m.cl_first = -1;
-        m.cl_size = 0;
-        return;
-    }
-    const int cs = cluster_setup<T>();
-    if (cs == 0) { m.cl_first = -1; m.cl_size = 0; return; }
-    P.nlev = L - first;
-    P.deg = m.deg_coarse;
-    for (int l = first; l < L; ++l) {
-        StencilLevel& S = m.lev[l - 1];
-        MGWork& w = m.work[l];
-        DevTransfer& tr = m.T[l];
-        ClusterLevel<T>& c = P.lev[l - first];
-        c.cx = S.cx;
-        c.cy = S.cy;
-        c.A = Sel<T>::A(S);
-        c.Dinv = Sel<T>::Di(S);
-        c.x = Sel<T>::x(w);
-        c.b = Sel<T>::b(w);
-        c.r = Sel<T>::r(w);
-        c.d = Sel<T>::d(w);
-        c.t = Sel<T>::t(w);
-        const double lmax = S.lmax, lmin = lmax / m.lo_ratio;
-        const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
-        double rho = 1.0 / sigma;
-        c.inv_theta = (T)(1.0 / theta);
-        for (int k = 1; k < m.deg_coarse; ++k) {   // the same recurrence as chebyshev()
-            const double rho_new = 1.0 / (2.0 * sigma - rho);
-            c.c1[k] = (T)(rho_new * rho);
-            c.c2[k] = (T)(2.0 * rho_new / delta);
-            rho = rho_new;
-        }
-        c.ncx = tr.ncx;
-        c.ncy = tr.ncy;
-        c.px = tr.px.p; c.py = tr.py.p; c.wx = Sel<T>::wx(tr); c.wy = Sel<T>::wy(tr);
-        c.rpx = tr.rpx.p; c.rix = tr.rix.p; c.rpy = tr.rpy.p; c.riy = tr.riy.p;
-        c.rwx = Sel<T>::rwx(tr); c.rwy = Sel<T>::rwy(tr);
-    }
-    StencilLevel& C = m.lev[L - 1];
-    P.nc = m.nc;
-    P.dcx = C.cx;
-    P.Cinv = Sel<T>::C(m);
-    P.xd = Sel<T>::x(m.work[L]);
-    P.bd = Sel<T>::b(m.work[L]);
-    m.cl_first = first;
-    m.cl_size = cs;
-}
-
 void mg_build(Handle& h) {
     mg_destroy(h);
     h.mg = new MGHier();
@@ -677,8 +609,6 @@ void mg_build(Handle& h) {
     m.lmax0 = estimate_lmax(h, 0);
     for (size_t k = 0; k + 1 < m.lev.size(); ++k) m.lev[k].lmax = estimate_lmax(h, (int)k + 1);
     EQC_CUDA(cudaStreamSynchronize(s));
-    setup_cluster_cycle<float>(h);
-    setup_cluster_cycle<double>(h);
     // the V-cycle recursion below the coarsest smoothed level uses lev[L-1] as the dense level
 }
 

@@ -50,33 +50,6 @@ struct MGWork {                  // per-level vectors, full layout of the level
     DBuf<float> x32, b32, r32, d32, t32;
 };
 
-// One level of the cluster-resident coarse cycle (mg_cluster.cu), with the transfer to the
-// next coarser level.
-constexpr int CL_MAXLEV = 8, CL_MAXDEG = 8;
-template <class T>
-struct ClusterLevel {
-    int cx, cy;                        // grid incl. the fault row; pitch cx
-    const T* A;                        // [9][cx*cy]
-    const T* Dinv;
-    T *x, *b, *r, *d, *t;
-    T inv_theta;                       // Chebyshev: first step 1/theta, step k: c1[k], c2[k]
-    T c1[CL_MAXDEG], c2[CL_MAXDEG];
-    int ncx, ncy;                      // next level
-    const int *px, *py;                // prolongation: 2 coarse neighbours per fine index
-    const T *wx, *wy;
-    const int *rpx, *rix, *rpy, *riy;  // restriction lists per coarse index
-    const T *rwx, *rwy;
-};
-template <class T>
-struct ClusterArgs {
-    int nlev, deg;
-    ClusterLevel<T> lev[CL_MAXLEV];
-    int nc, dcx;                       // dense coarsest: unknowns, row length (row 0 skipped)
-    const T* Cinv;
-    T *xd, *bd;
-};
-template <class T> int cluster_setup();   // cluster size usable on this device (0: none)
-template <class T> void cluster_cycle(const ClusterArgs<T>& P, int cluster, cudaStream_t s);
 
 struct MGHier {
     int deg = 4;          // Chebyshev steps on the spectral-element level
@@ -93,10 +66,6 @@ struct MGHier {
     DBuf<double> Cinv64;
     DBuf<float> Cinv32;
     int64_t launches_per_vcycle = 0;
-    // levels >= cl_first (work indexing) run inside one cluster launch (cl_size CTAs)
-    int cl_first = -1, cl_size = 0;
-    ClusterArgs<float> ca32{};
-    ClusterArgs<double> ca64{};
 };
 
 // host setup helpers (mg_setup.cpp)

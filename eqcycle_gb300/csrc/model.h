@@ -94,6 +94,8 @@ struct Handle {
     int64_t gen = 0;
     double setup_ms[5] = {0, 0, 0, 0, 0};
     int64_t pdl_edges = 0;   // programmatic kernel-to-kernel edges in the captured graphs
+    int tma_wait_polls = MBAR_SPIN_LIMIT;   // first-tile wait bound of the TMA applies (testing)
+    int64_t cap_time = 1900000;              // capacity of time_ / Vfmax (main.jl:154-163)
     // V-cycle pointwise work fused into the operator kernels (EQC_NO_FUSE set at creation: the
     // separate kernels, for comparisons)
     bool fuse = true;   // eqc_create phases: numbering, elements, nodes, other, hierarchy
@@ -182,10 +184,11 @@ template <class T>
 void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStream_t s);
 
 inline ApplyArgs<double> args64(Handle& h) {
-    return {h.W64.p, h.c1, h.c2, h.L, h.W64p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant};
+    return {h.W64.p, h.c1, h.c2, h.L, h.W64p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant, h.tma_wait_polls};
 }
 inline ApplyArgs<float> args32(Handle& h) {
-    return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant};
+    return {h.W32.p, (float)h.c1, (float)h.c2, h.L, h.W32p.p, &h.ctrl.p->apply_err, &h.tma, h.opt.apply_variant,
+            h.tma_wait_polls};
 }
 void tma_init(Handle& h);
 void set_H_df(const double* H, cudaStream_t s);
@@ -211,6 +214,8 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry = fa
 // Marks the carried residual stale (after the state was changed from outside the loop).
 void invalidate_residual(Handle& h);
 int qs_solve_device(Handle& h, double tol, int maxit, double* relres);
+// Throws EQC_E_TIMEOUT (and clears the device flag) when a TMA apply gave up a bounded wait.
+void check_apply_err(Handle& h);
 
 // graph.cu
 // Handle of a conditional node of the graph h.stream is capturing (value 0 at each launch

@@ -573,13 +573,23 @@ void invalidate_residual(Handle& h) {
 int qs_solve_device(Handle& h, double tol, int maxit, double* relres) {
     enqueue_solve(h, tol, maxit, false);
     const CGState& S = read_cg(h);
-    int err = 0;
-    EQC_CUDA(cudaMemcpyAsync(&err, &h.ctrl.p->apply_err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
-    EQC_CUDA(cudaStreamSynchronize(h.stream));
-    if (err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
+    check_apply_err(h);
     if (S.done == 3) throw Error(EQC_E_NAN, "non-finite residual in CG");
     if (relres) *relres = S.nb > 0 ? S.res / S.nb : S.res;
     return S.done == 1 ? S.it : -S.it;
+}
+
+// Reports (EQC_E_TIMEOUT) and clears the flag a TMA-fed apply sets when a bounded wait gave up,
+// so that the handle stays usable after the error.
+void check_apply_err(Handle& h) {
+    int err = 0;
+    EQC_CUDA(cudaMemcpyAsync(&err, &h.ctrl.p->apply_err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    EQC_CUDA(cudaStreamSynchronize(h.stream));
+    if (!err) return;
+    EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->apply_err, 0, sizeof(int), h.stream));
+    EQC_CUDA(cudaStreamSynchronize(h.stream));
+    h.h_ctrl->apply_err = 0;
+    throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
 }
 
 }  // namespace eqc

@@ -328,9 +328,11 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
     // Vfmax and its first index, the regime of the next step
     double vmax = -INFINITY;
     int imax = 0x7fffffff;
+    int nan = 0;   // Julia's maximum propagates NaN: so does Vfmax here
     for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) {
         const double vk = v[k];
         if (vk > vmax) { vmax = vk; imax = k; }
+        if (vk != vk) nan = 1;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -339,12 +341,13 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
         if (ov > vmax || (ov == vmax && oi < imax)) { vmax = ov; imax = oi; }
     }
     if (lane == 0) { smax[w] = vmax; sidx[w] = imax; }
-    __syncthreads();
+    const int anynan = __syncthreads_or(nan);
     if (threadIdx.x == 0) {
         double bv = -INFINITY;
         int bi = 0x7fffffff;
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q)
             if (smax[q] > bv || (smax[q] == bv && sidx[q] < bi)) { bv = smax[q]; bi = sidx[q]; }
+        if (anynan) { bv = __longlong_as_double(0x7ff8000000000000LL); bi = 0; }
         const double Vfmax = 2 * bv + Vpl;
         C->Vfmax = Vfmax;
         C->vhypo = Vfmax;
@@ -606,7 +609,7 @@ void init_state(Handle& h, double V_init) {
 }
 
 // capacities of the reference's preallocated outputs (main.jl:154-163)
-constexpr int64_t CAP_SEISMIC = 30000, CAP_IS = 4000, CAP_SEIS = 190000, CAP_EV = 400, CAP_TIME = 1900000;
+constexpr int64_t CAP_SEISMIC = 30000, CAP_IS = 4000, CAP_SEIS = 190000, CAP_EV = 400;
 constexpr int STEP_BATCH = 512;   // default steps per batched launch (the size of the device logs)
 
 static void fault_columns(Handle& h, std::vector<double>& dF, std::vector<double>& vF, std::vector<double>& tauF) {
@@ -871,10 +874,12 @@ void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb, bool logg
         else stats.dyn_steps++;
     }
     const double tnow = C.t;
+    if (!logged && (int64_t)h.res.time_.size() >= h.cap_time)
+        throw Error(EQC_E_CAPACITY, "time_ capacity (" + std::to_string(h.cap_time) + ") exceeded");
     if (!logged) h.res.time_.push_back(tnow);
     if (C.fail != 0x7fffffff)
         throw Error(EQC_E_NR, "NR SEARCH FAILED at fault node " + std::to_string(C.fail));
-    if (C.apply_err) throw Error(EQC_E_TIMEOUT, "stiffness apply: bounded wait for a TMA tile gave up");
+    if (C.apply_err) check_apply_err(h);
     if (C.cg_fail & 2) throw Error(EQC_E_NAN, "non-finite residual in CG");
     if (C.cg_fail & 1)
         throw Error(EQC_E_CG, "CG did not converge within maxit (relres " + std::to_string(C.cg_last_relres) + ")");
@@ -984,7 +989,8 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
     EQC_CUDA(cudaEventRecord(ev0, s));
     const int batch = h.opt.step_batch == 0 ? STEP_BATCH : h.opt.step_batch;
     while (C.t < t_end && stats.steps < max_steps) {
-        if ((int64_t)h.res.time_.size() >= CAP_TIME) throw Error(EQC_E_CAPACITY, "time_ capacity (1900000) exceeded");
+        if ((int64_t)h.res.time_.size() >= h.cap_time)
+            throw Error(EQC_E_CAPACITY, "time_ capacity (" + std::to_string(h.cap_time) + ") exceeded");
         const int iso = C.isolver;
         if (h.opt.use_graphs && batch > 1) {   // several steps per launch, outputs logged on the device
             const long long it_before = C.cg_iters, up_before = C.cg_updates, ca_before = C.cg_carried,
@@ -999,7 +1005,7 @@ void run_steps(Handle& h, int64_t max_steps, double t_end, eqc_run_stats* st) {
             C.idelevne = (int)h.idelevne;
             C.verbose = h.opt.verbose;
             C.max_batch = (int)std::min<int64_t>({(int64_t)batch, max_steps - stats.steps,
-                                                  CAP_TIME - (int64_t)h.res.time_.size()});
+                                                  h.cap_time - (int64_t)h.res.time_.size()});
             C.rec_cap = (int)std::min<int64_t>(STEP_BATCH / 10 + 2, CAP_SEIS - h.rit);
             if (h.nSeis > 0 && C.rec_cap < 1) throw Error(EQC_E_CAPACITY, "receiver capacity (190000) exceeded");
             C.nlog = 0;

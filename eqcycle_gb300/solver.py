@@ -57,7 +57,7 @@ class Solver:
                  guess: int = L.EQC_GUESS_PREVIOUS, cg_tol: float = 1e-8, cg_maxit: int = 0,
                  tol_rule: int = L.EQC_TOL_RHS, device: int = 0, use_graphs: int = 1, verbose: int = 0,
                  reliable_delta: float = 0.0, mg_degree: int = 0, mg_coarse_max: int = 0,
-                 mg_cluster_max: int = 0, apply_variant: int = 0, mg_degree_coarse: int = 0, step_batch: int = 0):
+                 apply_variant: int = 0, mg_degree_coarse: int = 0, step_batch: int = 0):
         self.P = P
         lib = L.lib()
         fa, ia, m = P.farray, P.iarray, P.mesh
@@ -96,7 +96,7 @@ class Solver:
                                          cg_maxit=cg_maxit, tol_rule=tol_rule, device=device,
                                          use_graphs=use_graphs, verbose=verbose, reliable_delta=reliable_delta,
                                          mg_degree=mg_degree, mg_coarse_max=mg_coarse_max,
-                                         mg_cluster_max=mg_cluster_max, apply_variant=apply_variant,
+                                         apply_variant=apply_variant,
                                          mg_degree_coarse=mg_degree_coarse, step_batch=step_batch)
         h = C.c_void_p()
         if structured:

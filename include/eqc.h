@@ -5,7 +5,7 @@
  * The reference (thehalfspace/eqcycle, Julia) has no FFI: its hot path is the
  * Julia function main(P) (src/main.jl:67-477) with P built by setParameters
  * (par.jl:15-231).  These entry points are what a Julia `ccall` shim keeping
- * main(P)'s signature binds (the shim is shown in INTEGRATION.md).  Every
+ * main(P)'s signature binds.  Every
  * entry point takes plain pointers and sizes; host arrays use the reference's
  * layouts (Julia column-major, node indices 1-based, reference node numbering
  * of src/MeshBox.jl:27-88).  The library copies what it needs and never keeps
@@ -91,8 +91,6 @@ typedef struct {
     int32_t mg_degree;      /* Chebyshev smoothing steps on the spectral-element level, pre and
                                post (default 4)                                        */
     int32_t mg_coarse_max;  /* largest coarsest level, solved densely (default 2048 unknowns) */
-    int32_t mg_cluster_max; /* > 0: levels with at most this many grid points run as one
-                               thread-block-cluster launch (default 0: off)            */
     int32_t apply_variant;  /* stiffness apply kernel: 0 default (FP32: one element per lane,
                                6 element rows per CTA; FP64: persistent TMA pipeline),
                                1 one tile per CTA by TMA, 2 plain tile loads, 3 persistent
@@ -260,7 +258,15 @@ eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
  * "setup_ms_other", "setup_ms_hierarchy" (the multigrid hierarchy), and "pdl_edges", the
  * kernel-to-kernel edges of the captured step graphs launched as programmatic dependent
  * launches (0 with the environment variable EQC_NO_PDL set at capture)).
- * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables). */
+ * eqc_set_scalar sets "t", "dt" or "isolver" of the state (main.jl's loop variables), after
+ * eqc_init.  Two settings of the handle are read and set the same way, at any time:
+ * "time_capacity", the length of the time_ / Vfmax records (default 1,900,000, the
+ * reference's preallocation, main.jl:154-163; eqc_run returns EQC_E_CAPACITY when a step
+ * would exceed it), and "tma_wait_polls", the bound, in polls, of the first tile wait of the
+ * TMA-fed stiffness applies (default and maximum 4,194,304; every later wait keeps that bound).
+ * A kernel whose wait runs out flags it, waits with the full bound for the copies it issued
+ * and returns; the call reports EQC_E_TIMEOUT and the handle stays usable.  Setting it to 0
+ * makes every TMA apply give up at once: that is how the failure path is tested. */
 eqc_status eqc_get_scalar(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_scalar(eqc_handle* h, const char* name, double value);
 

@@ -1,10 +1,12 @@
 """FP32 stiffness-apply kernels against each other and against the FP64 apply.
 
-The element-per-lane kernels (one CTA per tile of element rows, and the TMA-fed walk up the
-strips) share their arithmetic and the order in which neighbouring contributions are added, so
+The element-per-lane kernels (one CTA per tile of 4, 6, 8 or 12 element rows, and the TMA-fed
+walk up the strips) share their arithmetic and the order in which neighbouring contributions are added, so
 their outputs must agree bit for bit on every mesh shape: strips that end inside the mesh,
 walks of one and of several tiles, and the virtual last element row and column.  Against the
-FP64 apply the FP32 result agrees to FP32 rounding (1e-5 of the largest entry).
+FP64 apply the FP32 result agrees to FP32 rounding (1e-5 of the largest entry), as does that of
+the node-line kernels (apply variants 1-3: one TMA tile per CTA, plain tile loads, the persistent
+TMA pipeline), which sum the two element rows of a shared node row before contracting.
 """
 import ctypes as C
 
@@ -37,7 +39,7 @@ def test_fp32_apply_kernels_agree(eqclib, name):
     torch = pytest.importorskip("torch")
     P = set_parameters(MESHES[name])
     out = {}
-    for variant in (0, 8):
+    for variant in (0, 4, 5, 6, 7, 8, 1, 2, 3):
         with Solver(P, precond=EQC_PC_JACOBI, apply_variant=variant) as s:
             nx, ny, ld = s.layout()
             g = torch.Generator().manual_seed(7)
@@ -47,10 +49,13 @@ def test_fp32_apply_kernels_agree(eqclib, name):
             if variant == 0:
                 out["f64"] = _apply(s, torch, x.double(), 0)
             assert np.array_equal(_apply(s, torch, x, 1), out[variant])   # deterministic
-    assert np.array_equal(out[0], out[8])
-    y32, y64 = out[8][:, :nx].astype(np.float64), out["f64"][:, :nx]
-    assert np.max(np.abs(y32 - y64)) <= 1e-5 * np.max(np.abs(y64))
-    assert not np.any(out[8][:, nx:])   # row padding untouched
+    for v in (4, 5, 6, 7, 8):            # element per lane: row tiles of 4-12 rows, the TMA walk
+        assert np.array_equal(out[0], out[v]), v
+    y64 = out["f64"][:, :nx]
+    for v in (0, 1, 2, 3):               # and the node-line kernels: one TMA tile, plain loads, pipeline
+        y32 = out[v][:, :nx].astype(np.float64)
+        assert np.max(np.abs(y32 - y64)) <= 1e-5 * np.max(np.abs(y64)), v
+        assert not np.any(out[v][:, nx:]), v   # row padding untouched
 
 
 @pytest.mark.parametrize("variant", [0, 8])
