@@ -14,13 +14,22 @@ Methods: the headline runs the mixed-precision solver (FP32 stiffness apply and 
 inside an FP64 reliable-update CG, FP64 friction and state); the plain FP64 method runs the
 same window and is reported beside it.  Both stop CG at ||r|| <= 1e-8 ||b||.
 
+Beside the headline the default line carries, untimed: `mixed_error`, the mixed method's
+per-step error against the plain FP64 method (lockstep runs from the same start, quasi-static
+window and Newmark steps from a fast start), and `whole_cycle`, both methods over the first 20
+simulated years of the workload from the seeded start (interseismic steps, the nucleation, the
+first event's rupture and dynamic phase, afterslip), with the event statistics compared.
+
 --impl reference times the reference's algorithm on the host cores: the CPU oracle in
 reference mode (Ruge-Stueben AMG with Gauss-Seidel V-cycle inside CG, FP64 friction), the
 restatement of the Julia code (Julia is not installed here, so `julia run.jl` itself cannot
-run).  Its steps are whole QS steps, as many as fit in a time budget.
+run).  Its steps are whole QS steps from the seeded start, at least 3, more within a time
+budget; the default line's `cpu_baseline` is the same sample (at least 2 steps), taken in a
+spawned process while the GPU runs the untimed legs.
 
-N > 1 GPUs: the single-model path does not shard (replicas only); every rank advances its
-own replica and value sums the ranks' simulated years over the slowest rank's time.
+N > 1 GPUs (launched by torchrun, one rank per GPU; --gpus must equal WORLD_SIZE): the
+single-model path does not shard (replicas only); every rank advances its own replica and
+value sums the ranks' simulated years over the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -212,10 +221,11 @@ def run_window(P, precision, W, K, device, params=None, **kw):
     return s, st, sim_years, launches
 
 
-def cpu_baseline_sample(P, budget_s=240.0, min_steps=1):
-    """The oracle in reference mode on the host cores: whole QS steps from the same start."""
+def cpu_baseline_sample(P, budget_s=240.0, min_steps=1, nthreads=None, name="dz480"):
+    """The oracle in reference mode on the host cores: whole QS steps from the same start, at
+    least min_steps of them, more while the time spent stays within half the budget."""
     from oracle import pyoracle
-    nthreads = os.cpu_count() or 1
+    nthreads = nthreads or os.cpu_count() or 1
     pyoracle.set_threads(nthreads)
     o = pyoracle.Oracle(P.cfg)
     # same start as the GPU window: t = 0, dt = the steady dtevol! step
@@ -226,21 +236,157 @@ def cpu_baseline_sample(P, budget_s=240.0, min_steps=1):
     t_setup = time.time()
     o.qs_solve(np.zeros(o.Nf), np.zeros(o.nglob), tol=1e-8, mode=0, maxit=1)  # builds the AMG hierarchy
     setup_s = time.time() - t_setup
-    steps, wall, t0 = 0, 0.0, o.scalar("t")
-    while steps < min_steps or wall < budget_s * 0.5:
+    steps, wall, t0, per_step = 0, 0.0, o.scalar("t"), []
+    while True:
         t1 = time.time()
         n = o.run(1, qs_mode=0, qs_tol=1e-8)
-        wall += time.time() - t1
+        per_step.append(time.time() - t1)
+        wall += per_step[-1]
         steps += n
-        if n == 0 or wall > budget_s:
+        if n == 0 or (steps >= min_steps and wall + wall / steps > budget_s):
             break
     sim_years = (o.scalar("t") - t0) / YR
     cg = o.get("cg_iters")
     return {"value": sim_years / (wall / 3600.0), "unit": "sim-years/hr", "cores": nthreads, "kind": "port",
-            "sample": f"{steps} interseismic QS step(s) of dz480 from the seeded start (dt {dt_s:.3g} s), "
-                      f"oracle reference mode: RS-AMG + symmetric Gauss-Seidel V-cycle in CG to 1e-8, "
-                      f"{int(cg.sum())} CG iterations, {wall:.1f} s wall, AMG setup {setup_s:.1f} s excluded",
-            "steps": steps, "wall_s": wall, "sim_years": sim_years}
+            "sample": f"the first {steps} interseismic QS steps of {name} from the seeded start (dt "
+                      f"{dt_s:.3g} s), the oracle in reference mode (RS-AMG + symmetric Gauss-Seidel V-cycle in CG "
+                      f"to 1e-8, FP64 friction), {int(cg.sum())} CG iterations, {wall:.1f} s wall "
+                      f"(per step {', '.join(f'{x:.0f}' for x in per_step)} s); value = simulated years of these "
+                      f"steps over their wall time, no extrapolation; AMG setup {setup_s:.1f} s excluded",
+            "steps": steps, "wall_s": wall, "sim_years": sim_years, "per_step_s": per_step,
+            "cg_iters_per_solve": float(cg.sum()) / max(1, 2 * steps)}
+
+
+def _cpu_baseline_child(workload, budget_s, min_steps, nthreads, q):
+    """cpu_baseline_sample in a spawned process (the oracle only: no CUDA in this process), so
+    that the host-core sample runs while the GPU legs run in the parent."""
+    try:
+        from eqcycle_gb300 import preset, set_parameters
+        P = set_parameters(preset(workload))
+        q.put(cpu_baseline_sample(P, budget_s=budget_s, min_steps=min_steps, nthreads=nthreads, name=workload))
+    except Exception as e:  # reported in the JSON line instead of the sample
+        q.put({"error": repr(e)})
+
+
+def start_cpu_baseline(workload, budget_s, min_steps, nthreads):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    p = ctx.Process(target=_cpu_baseline_child, args=(workload, budget_s, min_steps, nthreads, q), daemon=True)
+    p.start()
+    return p, q
+
+
+def finish_cpu_baseline(job, timeout_s):
+    p, q = job
+    try:
+        res = q.get(timeout=timeout_s)
+    except Exception:
+        res = {"error": "CPU sample did not finish in time"}
+    p.join(timeout=10)
+    if p.is_alive():
+        p.kill()
+    return res
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
+
+def mixed_error_leg(P, device, W, K, dyn_steps=300):
+    """Per-step error of the mixed-precision method against the plain FP64 method on the
+    workload, both from the same start and stepped in lockstep (one step per call, outside any
+    timed region): after each of W + K interseismic quasi-static steps from the steady-sliding
+    start, and after each of dyn_steps Newmark steps from a fast start (the fault sliding at
+    5 cm/s, the dynamic regime).  Errors are max-norm relative to the FP64 field: the whole
+    displacement field d, the fault slip (2 d + Vpl t on the fault), the fault slip rate
+    (2 v + Vpl) and the state psi; the maximum over the steps is reported."""
+    from eqcycle_gb300 import EQC_FP64, EQC_GUESS_EXTRAPOLATE, EQC_MIXED, Solver
+    iF = P.iarray.iFlt - 1
+    Vpl = P.float_.Vpl
+    out = {}
+    for phase in ("quasi_static", "dynamic"):
+        a = Solver(P, precision=EQC_FP64, cg_tol=1e-8, device=device)
+        b = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device, guess=EQC_GUESS_EXTRAPOLATE)
+        n = W + K if phase == "quasi_static" else dyn_steps
+        err = {"d": 0.0, "slip": 0.0, "slip_rate": 0.0, "psi": 0.0}
+        for s in (a, b):
+            if phase == "quasi_static":
+                s.init(P.cfg.V_init)
+                s.set_scalar("dt", steady_dt(s, P))
+            else:
+                s.init(5e-2)
+        regimes = set()
+        for k in range(n):
+            sa, sb = a.run(1), b.run(1)
+            regimes.add(int(sa["dyn_steps"]) * 2 + int(sa["qs_steps"]))
+            t = a.scalar("t")
+            full = phase == "quasi_static" or k % 25 == 24 or k == n - 1
+            da = a.state("d") if full else None
+            db = b.state("d") if full else None
+            va, vb = a.state("v")[iF], b.state("v")[iF]
+            if full:
+                err["d"] = max(err["d"], _rel(db, da))
+                err["slip"] = max(err["slip"], _rel(2 * db[iF] + Vpl * t, 2 * da[iF] + Vpl * t))
+            err["slip_rate"] = max(err["slip_rate"], _rel(2 * vb + Vpl, 2 * va + Vpl))
+            err["psi"] = max(err["psi"], _rel(b.state("psi"), a.state("psi")))
+        out[phase] = {"steps": n, "regime": "dynamic" if regimes == {2} else "quasi-static" if regimes == {1}
+                      else "mixed", **{f"max_rel_err_{k}": v for k, v in err.items()}}
+        a.close()
+        b.close()
+    out["note"] = ("mixed (FP32 apply and multigrid in an FP64 reliable-update CG to 1e-8; FP64 friction, state "
+                   "and Newmark accumulation) against plain FP64 (CG to 1e-8), same start, compared after every "
+                   "step; displacement field every step in the quasi-static phase, every 25 steps in the "
+                   "dynamic one")
+    return out
+
+
+def cycle_leg(P, device, years=20.0, budget_s=400.0):
+    """Whole earthquake cycle on the workload: the plain FP64 method and the mixed method
+    (extrapolated guess, smoother autotuned after its first 20 quasi-static steps) each run the
+    simulation from the seeded start to t = `years` (the dz480 model nucleates at about 1.5 yr
+    and its first event ends near 7 yr: the window holds the interseismic start, the nucleation,
+    the rupture and its dynamic phase, the afterslip and the return to interseismic steps), or
+    until budget_s seconds of wall time.  value = simulated years per hour of device time (CUDA
+    events); event statistics of the two runs are compared (first event start, coseismic slip,
+    hypocentre depth, Mw)."""
+    from eqcycle_gb300 import EQC_FP64, EQC_GUESS_EXTRAPOLATE, EQC_GUESS_PREVIOUS, EQC_MIXED, Solver
+    from eqcycle_gb300.events import catalogue, compare
+    mu = P.cfg.rho1 * P.cfg.vs1 ** 2
+    out, cats = {}, {}
+    t_stop = years * YR
+    for name, prec, guess in (("plain_fp64", EQC_FP64, EQC_GUESS_PREVIOUS), ("mixed", EQC_MIXED, EQC_GUESS_EXTRAPOLATE)):
+        with Solver(P, precision=prec, cg_tol=1e-8, guess=guess, device=device) as s:
+            s.init(P.cfg.V_init)
+            gpu_ms, qs, dyn, cg, solves, wall0, tuned = 0.0, 0, 0, 0, 0, time.time(), None
+            while s.scalar("t") < t_stop and time.time() - wall0 < budget_s:
+                st = s.run(5000, t_stop)
+                gpu_ms += st["gpu_ms"]
+                qs += st["qs_steps"]
+                dyn += st["dyn_steps"]
+                cg += st["cg_iters"]
+                solves += st["qs_solves"]
+                if prec == EQC_MIXED and tuned is None and qs >= 20:
+                    tuned = s.autotune(reps=2)
+            years_run = s.scalar("t") / YR
+            res = s.results()
+        cats[name] = catalogue(res, P.farray.FltX, mu)
+        out[name] = {"sim_years": years_run, "value": years_run / (gpu_ms / 3.6e6) if gpu_ms else None,
+                     "gpu_s": gpu_ms / 1e3, "wall_s": time.time() - wall0, "qs_steps": qs, "dyn_steps": dyn,
+                     "cg_iters_per_solve": cg / max(solves, 1), "autotune": tuned, **cats[name].summary()}
+    a, b = cats["plain_fp64"], cats["mixed"]
+    cmp = compare(a, b)
+    if len(a.tStart) and len(b.tStart):
+        cmp["first_event_start"] = float(abs(b.tStart[0] - a.tStart[0]) / a.tStart[0])
+    if len(a.Mw) and len(b.Mw):
+        cmp["Mw_abs"] = float(np.max(np.abs(b.Mw[:len(a.Mw)] - a.Mw[:len(b.Mw)])))
+    out["event_statistics_mixed_vs_fp64"] = cmp
+    pv, mv = out["plain_fp64"]["value"], out["mixed"]["value"]
+    out["speedup_mixed_vs_plain_fp64"] = mv / pv if pv and mv else None
+    out["window"] = (f"t = 0 to {years:g} yr from the seeded start, both methods (first event "
+                     f"{a.tStart[0] / YR if len(a.tStart) else float('nan'):.2f} to "
+                     f"{a.tEnd[0] / YR if len(a.tEnd) else float('nan'):.2f} yr in the FP64 run)")
+    return out
 
 
 def bench_ours(args):
@@ -349,6 +495,15 @@ def bench_ours(args):
         learned["pairs"] = int(sum(len(x) for x in xs))
         learned["train_and_log_s"] = time.time() - t_l
         sl_.close()
+    # ---- the host-core sample of the reference's algorithm runs in a spawned process (no CUDA
+    # there) while the untimed legs below use the GPU; one core is left to drive the GPU
+    cpu_job = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu_job = start_cpu_baseline(args.workload, args.cpu_budget, args.cpu_min_steps,
+                                     max(1, (os.cpu_count() or 2) - 1))
+    mixed_error = mixed_error_leg(P, device, args.warmup, args.steps) if not args.no_cycle else None
+    whole_cycle = cycle_leg(P, device, years=args.cycle_leg_years, budget_s=args.cycle_leg_budget) \
+        if not args.no_cycle else None
     if rank != 0:
         return
     line = {
@@ -387,8 +542,13 @@ def bench_ours(args):
     line["speedup_vs_plain_fp64"] = value / line["plain_fp64"]["value"] if line["plain_fp64"]["value"] else None
     if clk:
         line["clocks"] = clk
-    if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(P, budget_s=args.cpu_budget)
+    line["mixed_error"] = mixed_error
+    line["whole_cycle"] = whole_cycle
+    if cpu_job is not None:
+        cb = finish_cpu_baseline(cpu_job, timeout_s=3 * args.cpu_budget + 600)
+        if "error" not in cb:
+            cb["concurrent"] = "ran on the host cores while the GPU ran the untimed legs (mixed_error, whole_cycle)"
+        line["cpu_baseline"] = cb
     print(json.dumps(line), flush=True)
 
 
@@ -414,7 +574,10 @@ def bench_reference(args):
         return
     from eqcycle_gb300 import set_parameters, preset
     P = set_parameters(preset(args.workload))
-    cb = cpu_baseline_sample(P, budget_s=args.cpu_budget, min_steps=max(1, min(args.steps, 1)))
+    # whole QS steps of the reference algorithm: at least 3 (about 100 s each on 16 Arm cores: the
+    # symmetric Gauss-Seidel smoother of the reference's AMG is sequential), more within the budget
+    cb = cpu_baseline_sample(P, budget_s=max(args.cpu_budget, 360.0), min_steps=max(3, args.cpu_min_steps),
+                             name=args.workload)
     line = {"impl": "reference", "metric": "sim-years/hr", "value": cb["value"], "unit": "sim-years/hr",
             "n_gpus": ws, "steps": cb["steps"], "warmup": 0, "ms_per_step": 1e3 * cb["wall_s"] / max(cb["steps"], 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -650,7 +813,7 @@ def bench_cycle(args):
             res = s.results()
         cat = catalogue(res, P.farray.FltX, mu)
         cats[name] = cat
-        out[name] = {"sim_years": years, "value": years / (gpu_ms / 3.6e6) if gpu_ms else None,
+        out[name] = {"sim_years": years_run, "value": years_run / (gpu_ms / 3.6e6) if gpu_ms else None,
                      "gpu_s": gpu_ms / 1e3, "wall_s": time.time() - wall0, "qs_steps": qs, "dyn_steps": dyn,
                      "cg_iters_per_solve": cg / max(solves, 1), "autotune": tuned, **cat.summary()}
     line = {"metric": "sim-years/hr over whole cycles", "workload": wl, "years_target": t_end / YR,
@@ -666,8 +829,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=None, help="dz480 (default), dz960, homog48 (--cycle default), ...")
-    ap.add_argument("--cpu-budget", type=float, default=150.0)
+    ap.add_argument("--cpu-budget", type=float, default=240.0,
+                    help="host-core sample of the reference algorithm: wall seconds (whole QS steps)")
+    ap.add_argument("--cpu-min-steps", type=int, default=2, help="... and at least this many steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cycle", action="store_true",
+                    help="default run without the whole-cycle and mixed-error legs")
+    ap.add_argument("--cycle-leg-budget", type=float, default=300.0,
+                    help="default run: wall seconds per method of the whole-cycle leg")
+    ap.add_argument("--cycle-leg-years", type=float, default=20.0,
+                    help="default run: simulated years of the whole-cycle leg (from the seeded start)")
     ap.add_argument("--kernel-only", action="store_true", help="time the stiffness apply alone")
     ap.add_argument("--setup", action="store_true", help="time the model setup, host against device")
     ap.add_argument("--profile-steps", action="store_true",
@@ -695,6 +866,12 @@ def main():
                     help="stiffness apply kernel: 0 default, 1 one tile per CTA (TMA), 2 plain tile loads, "
                          "3 persistent TMA pipeline, 4-7 element per lane with 4/8/12/6 rows per CTA, 8 TMA walk")
     args = ap.parse_args()
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != ws:
+        # one process per GPU: N > 1 ranks come from torchrun, which sets WORLD_SIZE
+        sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={ws}; for N > 1 launch one rank per GPU with "
+                 f"python -m torch.distributed.run --nnodes=1 --nproc-per-node {args.gpus} "
+                 f"--master-addr 127.0.0.1 --master-port <port> bench.py --gpus {args.gpus} ...")
     if args.workload is None and not args.cycle:
         args.workload = "dz480"
     if args.kernel_only:

@@ -58,7 +58,7 @@ __device__ __forceinline__ int dev_NR(double fo, double Vo, double cca, double c
     return 0;
 }
 
-// Closed-form quasi-static slip rate of slrFunc! (src/otherFunctions_serial.jl:171-176).
+// Closed-form quasi-static slip rate of slrFunc! (src/otherFunctions_serial.jl:74-78).
 __device__ __forceinline__ double dev_slr_V(double fo, double Vo, double cca, double ccb, double Seff, double tauo,
                                             double tau1, double psi1) {
     const double tauAB = tau1 + tauo;

@@ -8,7 +8,7 @@ assembled ``Ksparse``.  Setup runs once per model and is not on the hot path.
 
 Cited reference pieces: GetGLL.jl:17-28 (GLL tables), MeshBox.jl:27-88 (numbering and
 coordinates), Assemble.jl:7-71 (mass, dt, muMax), MaterialProperties.jl:3-21 / 77-101 (W),
-BoundaryMatrix.jl:7-61, FindNearestNode.jl:3-19, defaultInitialConditions.jl:169-251
+BoundaryMatrix.jl:7-61, FindNearestNode.jl:3-19, defaultInitialConditions.jl:9-84
 (depth profiles), par.jl:304-339 (XiLf).
 """
 from __future__ import annotations
@@ -161,7 +161,7 @@ class Params:
 
 # --------------------------------------------------------------------------- setup
 def _int1d(p1v, p1z, p2v, p2z, val):
-    # defaultInitialConditions.jl:169-172
+    # Int1D, defaultInitialConditions.jl:2-5
     return p1v + ((p2v - p1v) / (p2z - p1z)) * (val - p1z)
 
 

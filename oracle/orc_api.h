@@ -30,7 +30,7 @@ extern "C" {
  * generalised so that the workload presets (48x48 homogeneous, 480x240
  * damage zone, ...) and the reference's own defaults are all expressible. */
 typedef struct {
-    int32_t profile;   /* 0: reference depth profiles (defaultInitialConditions.jl:176-251)
+    int32_t profile;   /* 0: reference depth profiles (defaultInitialConditions.jl:9-84)
                           1: uniform a, tapered b, uniform sigma, seeded theta noise */
     int32_t damage;    /* 0: homogeneous; 1: rectangle, per element (MaterialProperties.jl:3-21);
                           2: trapezoid, per GLL node (mat_trap style, MaterialProperties.jl:77-101) */

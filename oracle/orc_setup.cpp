@@ -8,7 +8,7 @@
 //   stiffness            src/Kassemble.jl:3-63
 //   boundary matrices    src/BoundaryMatrix.jl:7-61
 //   receivers            src/FindNearestNode.jl:3-19
-//   depth profiles       src/initialConditions/defaultInitialConditions.jl:169-251
+//   depth profiles       src/initialConditions/defaultInitialConditions.jl:9-84
 //   XiLf                 par.jl:304-339
 #include "orc_internal.h"
 #include <cmath>
@@ -75,7 +75,7 @@ struct SplitMix {
 };
 
 static double Int1D(double p1v, double p1z, double p2v, double p2z, double val) {
-    // defaultInitialConditions.jl:169-172
+    // Int1D, defaultInitialConditions.jl:2-5
     return p1v + ((p2v - p1v) / (p2z - p1z)) * (val - p1z);
 }
 

@@ -2,15 +2,16 @@
 
 The table is the only data the reference ships for the hot path (GetGLL.jl:17-28 reads it:
 row 1 = nodes x, row 2 = weights w, rows 3-7 = H with H[i,j] = h'_i(x_j)).  It pins the
-oracle's and the product's GLL computation.  Run in a checkout where the reference is at
-REFERENCE (default /root/reference):  python tests/golden/make_gll_golden.py
+oracle's and the product's GLL computation.  Run with the root of a checkout of the reference:
+    python tests/golden/make_gll_golden.py <reference checkout>
 """
 import json
 import os
 import sys
 
-ref = os.environ.get("REFERENCE", "/root/reference")
-path = os.path.join(ref, "src", "gll_xwh", "gll_05.tab")
+if len(sys.argv) != 2:
+    sys.exit(__doc__)
+path = os.path.join(sys.argv[1], "src", "gll_xwh", "gll_05.tab")
 rows = []
 with open(path) as f:
     for line in f:

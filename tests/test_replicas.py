@@ -98,3 +98,16 @@ def test_ensemble_shards_over_gloo():
     for r, mask, tot, k in res:
         assert mask == [1.0] * 64 and tot == total and k > 0
     assert sum(k for _, _, _, k in res) == 64
+
+
+def test_bench_refuses_a_gpu_count_without_ranks():
+    """bench.py --gpus N needs one rank per GPU (torchrun sets WORLD_SIZE = N): a mismatch exits
+    with a message instead of reporting fewer GPUs than asked for."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--steps", "1"],
+                       capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0
+    assert "WORLD_SIZE=1" in r.stderr and "torch.distributed.run" in r.stderr
