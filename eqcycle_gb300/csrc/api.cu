@@ -21,6 +21,10 @@ Handle::~Handle() {
     if (h_cg) cudaFreeHost(h_cg);
     for (cudaStream_t c : cap_streams)
         if (c) cudaStreamDestroy(c);
+    for (cudaStream_t c : {side_stream, side_stream2})
+        if (c) cudaStreamDestroy(c);
+    for (cudaEvent_t e : {ev_fork, ev_join, ev_fork2, ev_join2})
+        if (e) cudaEventDestroy(e);
     if (own_stream) cudaStreamDestroy(own_stream);
 }
 
@@ -141,6 +145,10 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     EQC_CUDA(cudaSetDevice(h.opt.device));
     h.fuse = std::getenv("EQC_NO_FUSE") == nullptr;
     EQC_CUDA(cudaStreamCreateWithFlags(&h.own_stream, cudaStreamNonBlocking));
+    for (cudaStream_t* c : {&h.side_stream, &h.side_stream2})
+        EQC_CUDA(cudaStreamCreateWithFlags(c, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&h.ev_fork, &h.ev_join, &h.ev_fork2, &h.ev_join2})
+        EQC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     h.stream = h.own_stream;
     cudaStream_t s = h.stream;
     Layout& L = h.L;
@@ -178,10 +186,10 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
 
     // reference node -> layout index, from the connectivity (or MeshBox's numbering rule)
     h.ref2lay.resize(m.nglob);
-    constexpr int64_t CH = 1 << 16;
+    constexpr int64_t CH = 1 << 14;   // nodes per work item of the host loops
     parallel_for((m.nglob + CH - 1) / CH, [&](int64_t c) {
         std::fill(h.ref2lay.begin() + c * CH, h.ref2lay.begin() + std::min(m.nglob, (c + 1) * CH), (int64_t)-1);
-    });
+    }, 1);
     if (mat) {   // MeshBox's numbering is a bijection of the nx x ny nodes: rows write disjoint entries
         parallel_for(L.ny, [&](int64_t iy) {
             for (int64_t ix = 0; ix < L.nx; ++ix) h.ref2lay[meshbox_id(ix, iy, L.nx)] = iy * L.ld + ix;
@@ -203,7 +211,7 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
         std::vector<char> hole(nc, 0);
         parallel_for(nc, [&](int64_t c) {
             for (int64_t g = c * CH; g < std::min(m.nglob, (c + 1) * CH); ++g) hole[c] |= h.ref2lay[g] < 0;
-        });
+        }, 1);
         for (char x : hole) fail_if(x != 0, "iglob does not cover every node");
     }
     const int Nf = (int)m.FltNglob;
@@ -325,6 +333,36 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
     F.NFBC0 = nfbc;
     h.creep_prefix = true;
     for (auto g : lCreep) h.creep_prefix = h.creep_prefix && g < nfbc;
+    {   // the mixed method's four-kernel dynamic step needs iBcL on column ix = 0 and iBcT on row
+        // iy = ny - 1, each node listed once (the reference's BoundaryMatrix edges x = -LX, y = LY)
+        std::vector<double> cL(L.ny, 0.0), cT(L.nx, 0.0);
+        std::vector<int> hL(L.ny, 0), hT(L.nx, 0);
+        bool ok = h.creep_prefix;
+        for (size_t k = 0; k < lBcL.size() && ok; ++k) {
+            const int64_t g = lBcL[k], iy = g / L.ld, ix = g % L.ld;
+            ok = ix == 0 && iy < L.ny && !hL[iy];
+            if (ok) { hL[iy] = 1; cL[iy] = m.BcLC[k]; }
+        }
+        for (size_t k = 0; k < lBcT.size() && ok; ++k) {
+            const int64_t g = lBcT[k], iy = g / L.ld, ix = g % L.ld;
+            ok = iy == L.ny - 1 && ix < L.nx && !hT[ix];
+            if (ok) { hT[ix] = 1; cT[ix] = m.BcTC[k]; }
+        }
+        h.nm_fused = ok && std::getenv("EQC_NO_NM_FUSE") == nullptr;
+        if (h.nm_fused) {
+            h.edgeL0has = hL[0];
+            h.edgeL0 = cL[0];
+            h.fault_count.alloc(1);
+            h.fault_part.alloc(3 * (size_t)((Nf + 31) / 32));
+            up_d(h.edgeL, cL.data(), L.ny);
+            up_d(h.edgeT, cT.data(), L.nx);
+            h.edgeLhas.alloc(L.ny);
+            h.edgeLhas.upload(hL.data(), L.ny, s);
+            h.edgeThas.alloc(L.nx);
+            h.edgeThas.upload(hT.data(), L.nx, s);
+            EQC_CUDA(cudaStreamSynchronize(s));
+        }
+    }
     for (DBuf<double>* b : {&F.fo, &F.Vo, &F.xLf, &F.cca, &F.ccb, &F.Seff, &F.tauo, &F.XiLf, &F.FltB, &F.FltZ, &F.FltX,
                             &F.Mf, &F.psi, &F.psi1, &F.psi2, &F.tau, &F.tau1, &F.tau2, &F.Vf, &F.Vf0, &F.Vf1, &F.Vf2,
                             &F.FltVfree, &F.vPre, &F.Flast})
@@ -388,21 +426,21 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
 // Reference numbering <-> node layout on the host's cores: ref2lay is one-to-one, so the
 // chunks write disjoint entries (the layout's row padding stays zero).
 static void to_layout(const Handle& h, const double* ref, std::vector<double>& lay) {
-    constexpr int64_t CH = 1 << 16;
+    constexpr int64_t CH = 1 << 14;   // nodes per work item
     const int64_t N = h.L.size();
     lay.resize(N);
     parallel_for((N + CH - 1) / CH, [&](int64_t c) {
         std::fill(lay.begin() + c * CH, lay.begin() + std::min(N, (c + 1) * CH), 0.0);
-    });
+    }, 1);
     parallel_for((h.nglob + CH - 1) / CH, [&](int64_t c) {
         for (int64_t g = c * CH; g < std::min(h.nglob, (c + 1) * CH); ++g) lay[h.ref2lay[g]] = ref[g];
-    });
+    }, 1);
 }
 static void from_layout(const Handle& h, const std::vector<double>& lay, double* ref) {
-    constexpr int64_t CH = 1 << 16;
+    constexpr int64_t CH = 1 << 14;
     parallel_for((h.nglob + CH - 1) / CH, [&](int64_t c) {
         for (int64_t g = c * CH; g < std::min(h.nglob, (c + 1) * CH); ++g) ref[g] = lay[h.ref2lay[g]];
-    });
+    }, 1);
 }
 
 static thread_local std::string g_create_err;

@@ -125,6 +125,8 @@ struct ApplyArgs {
     int wait_polls;   // poll bound of a TMA kernel's first tile wait (the later waits and the
                       // drain after a give-up keep MBAR_SPIN_LIMIT); lowered only to test the
                       // give-up path (eqc_set_scalar "tma_wait_polls")
+    const int* gate = nullptr;   // when set, the launch does nothing unless *gate (written by a
+    int gate_val = 0;            // preceding kernel) equals gate_val
 };
 
 // Bound, in polls of mbarrier.try_wait, of every wait of the TMA-fed stiffness applies.

@@ -69,6 +69,7 @@ static void ensemble_capture(eqc_ensemble& E) {
                 cond_begin(h, cudaGraphCondTypeIf, reg == 1 ? hq : hd);
                 enqueue_step(h, reg, true);
                 cond_end(h);
+                h.pdl_off = false;
                 G.k_fixed = (capture_tally() - t0) - G.k_bodies + G.k_fixed_extra + 1;   // + the selector
                 h.capturing = nullptr;
             }

@@ -5,8 +5,28 @@
 // fused and the separate forms give the same bits.
 #pragma once
 #include <cuda_runtime.h>
+#include <cstdint>
+#if defined(__CUDACC__)
+#include "vec.cuh"
+#include "df.cuh"
+#endif
 
 namespace eqc {
+
+// The end of a mixed-precision Newmark step at one node off the fault row (main.jl:309-339),
+// given t = (K dd)_i, the FP32 apply of the step's displacement increment: K d += t (FP64),
+// a = -K d, the absorbing terms a -= C v of the nodes on the edge x = -LX (column ix = 0, list
+// iBcL) and on the edge y = LY (row iy = ny - 1, list iBcT) in that order, then a /= M (a
+// multiply by 1/M) and v += dt/2 a.  The fault row is ended by the dynamic step's fault kernel.
+struct NmEpi {
+    double *Kd = nullptr, *v = nullptr, *a = nullptr;
+    const double* invM = nullptr;
+    const double *cL = nullptr, *cT = nullptr;     // [ny] / [nx] coefficients on the two edges
+    const int *hasL = nullptr, *hasT = nullptr;    // ... and whether the node is in the list
+    const double* hdt = nullptr;                    // dt / 2 (in the control block)
+    const int* kd_full = nullptr;                   // nonzero: K d recomputed in FP64 this step
+    int ld = 0, nx = 0, ny = 0;
+};
 
 // What an operator kernel does with t = (A x)_i at the nodes it owns.
 template <class T>
@@ -42,6 +62,73 @@ __device__ __forceinline__ void cheb_step_pt(T& r, T& d, T& x, T t, T dinv, T c1
     r = fma_rn<T>(-dinv, t, r);
     d = fma_rn<T>(c1, d, mul_rn<T>(c2, r));
     x = add_rn<T>(x, d);
+}
+
+// FP32 -> FP64, exact, by integer operations on the bit patterns (GB300 converts to FP64 on its
+// FP64 unit, a small fraction of its integer and FP32 rate).  Zeros, subnormals, infinities
+// and NaNs included.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint64_t sign = (uint64_t)(b >> 31) << 63;
+    const uint32_t e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+    if (e == 0xffu) return __longlong_as_double((long long)(sign | (0x7ffull << 52) | ((uint64_t)m << 29)));
+    if (e != 0) return __longlong_as_double((long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29)));
+    if (m == 0) return __longlong_as_double((long long)sign);
+    const int p = 31 - __clz((int)m);                 // leading one of a subnormal: m * 2^-149
+    const uint64_t frac = ((uint64_t)m - (1ull << p)) << (52 - p);
+    return __longlong_as_double((long long)(sign | ((uint64_t)(p + 874) << 52) | frac));
+}
+
+// The FP32 increment dt vh of a dynamic step from the half-step velocity vh: vh rounded to FP32
+// (integer operations), times dt given as hi + lo in FP32, so the product is rounded once
+// without the systematic error of a rounded dt, which K d would accumulate step after step.
+__device__ __forceinline__ float nm_incr32(double vh, float dt_hi, float dt_lo) {
+    const df vd = df_from_double(vh);
+    const float v32 = __fadd_rn(vd.hi, vd.lo);
+    return __fmaf_rn(dt_hi, v32, __fmul_rn(dt_lo, v32));
+}
+
+// One node (ix, iy >= 1) of the Newmark end (NmEpi).  add: t is added to K d (else K d was just
+// recomputed in FP64).
+__device__ __forceinline__ void newmark_node(const NmEpi& N, int64_t i, int ix, int iy, float t, bool add,
+                                             double hdt) {
+    double kd = N.Kd[i];
+    if (add) {
+        kd = __dadd_rn(kd, f32_to_f64(t));
+        N.Kd[i] = kd;
+    }
+    double ai = -kd;
+    const double vi = N.v[i];
+    if (ix == 0 && N.hasL[iy]) ai = __dsub_rn(ai, __dmul_rn(N.cL[iy], vi));
+    if (iy == N.ny - 1 && N.hasT[ix]) ai = __dsub_rn(ai, __dmul_rn(N.cT[ix], vi));
+    ai = __dmul_rn(ai, N.invM[i]);
+    N.a[i] = ai;
+    N.v[i] = __fma_rn(hdt, ai, vi);
+}
+
+// Four consecutive nodes ix0 .. ix0 + 3 of row iy >= 1 (offset off, 32-byte aligned): 4-wide
+// accesses off the edges, node by node on them and at the row's end.
+__device__ __forceinline__ void newmark4(const NmEpi& N, int64_t off, int ix0, int iy, const float (&t)[4], bool add,
+                                         double hdt) {
+    if (ix0 + 3 >= N.nx || ix0 == 0 || iy == N.ny - 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (ix0 + q < N.nx) newmark_node(N, off + q, ix0 + q, iy, t[q], add, hdt);
+        return;
+    }
+    double kd[4], vv[4], im[4], aa[4];
+    ld4(N.Kd + off, kd);
+    ld4(N.v + off, vv);
+    ld4(N.invM + off, im);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (add) kd[q] = __dadd_rn(kd[q], f32_to_f64(t[q]));
+        aa[q] = __dmul_rn(-kd[q], im[q]);
+        vv[q] = __fma_rn(hdt, aa[q], vv[q]);
+    }
+    if (add) st4(N.Kd + off, kd);
+    st4(N.a + off, aa);
+    st4(N.v + off, vv);
 }
 
 // Four consecutive owned nodes starting at offset off (16-byte aligned, FP32).

@@ -58,6 +58,48 @@ __device__ __forceinline__ int dev_NR(double fo, double Vo, double cca, double c
     return 0;
 }
 
+// The mixed method's Newton search: NRsearch!'s iteration, stopping rule and failure statuses,
+// with the loop's constants hoisted (fa = s tau, Vf' = vp (help1 + help2), the right-hand side
+// FltZ FltVfree + tauo summed once) and explicit fused multiply-adds.  The caller starts it from
+// the node's current shear stress instead of 0: the function tau -> tauo + FltZ (FltVfree - Vf(tau))
+// - tau is concave and decreasing, so from a start left of the root the first step lands right of
+// it by the curvature over the distance, and from the right the iterates decrease monotonically
+// by about a sigma / fact per step while Vf is far above its root value.  From 0 the first step
+// overshoots by about FltZ Vf (megapascals at seismic slip rates, several a sigma), from the
+// current stress by the step's stress change: fewer iterations, the same root to within the
+// stopping tolerance 0.001 a sigma.
+__device__ __forceinline__ int dev_NR_warm(double fo, double Vo, double cca, double ccb, double Seff, double tau,
+                                           double tauo, double psi, double FltZ, double FltVfree, double* Vf_out,
+                                           double* tau_out) {
+    const double Vw = 1e10;
+    const double fact = 1. + (Vo / Vw) * exp(-psi);
+    const double eps = 0.001 * cca * Seff;
+    const double help = -(fo + ccb * psi) / cca;
+    const double s = fact / (Seff * cca);
+    const double vp = Vo * s;
+    const double rhs = __fma_rn(FltZ, FltVfree, tauo);
+    int k = 0;
+    double delta = __longlong_as_double(0x7ff0000000000000LL);  // +Inf
+    while (fabs(delta) > eps) {
+        const double fa = s * tau;
+        const double help1 = exp(help + fa);
+        const double help2 = exp(help - fa);
+        const double Vf = Vo * (help1 - help2);
+        delta = (__fma_rn(-FltZ, Vf, rhs) - tau) / __fma_rn(FltZ, vp * (help1 + help2), 1.0);
+        tau = tau + delta;
+        k = k + 1;
+        if (fabs(delta) > 1e10 || k == 1000) {
+            *Vf_out = Vf;
+            *tau_out = tau;
+            return fabs(delta) > 1e10 ? 2 : 1;
+        }
+    }
+    const double fa = s * tau;
+    *Vf_out = Vo * (exp(help + fa) - exp(help - fa));
+    *tau_out = tau;
+    return 0;
+}
+
 // Closed-form quasi-static slip rate of slrFunc! (src/otherFunctions_serial.jl:74-78).
 __device__ __forceinline__ double dev_slr_V(double fo, double Vo, double cca, double ccb, double Seff, double tauo,
                                             double tau1, double psi1) {

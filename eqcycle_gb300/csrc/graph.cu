@@ -72,6 +72,7 @@ void abort_capture(Handle& h) {
     }
     cudaGetLastError();
     h.stream = h.own_stream;
+    h.pdl_off = false;
     capture_counting(false);
 }
 
@@ -117,7 +118,7 @@ void cond_end(Handle& h) {
     if (h.stream_stack.empty()) throw Error(EQC_E_STATE, "cond_end without cond_begin");
     cudaGraph_t g = nullptr;
     EQC_CUDA(cudaStreamEndCapture(h.stream, &g));
-    h.pdl_edges += make_programmatic(g);
+    if (!h.pdl_off) h.pdl_edges += make_programmatic(g);
     h.stream = h.stream_stack.back();
     h.stream_stack.pop_back();
 }

@@ -7,11 +7,13 @@
 
 namespace eqc {
 
-// f(i) for i in [0, n), in contiguous chunks, one per thread (at most one thread per 16 items).
-// Callers write disjoint outputs, so results do not depend on the thread count; f must not throw.
+// f(i) for i in [0, n), in contiguous ranges, one per thread, with at least `grain` items per
+// thread (1 where every item is already a large chunk of work, e.g. 16K nodes).  Callers write
+// disjoint outputs, so results do not depend on the thread count; f must not throw.
 template <class F>
-void parallel_for(int64_t n, F&& f) {
-    const int64_t nt = std::max<int64_t>(1, std::min<int64_t>(std::thread::hardware_concurrency(), n / 16 + 1));
+void parallel_for(int64_t n, F&& f, int64_t grain = 16) {
+    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+    const int64_t nt = std::max<int64_t>(1, std::min<int64_t>(hw, n / std::max<int64_t>(grain, 1)));
     if (nt <= 1) {
         for (int64_t i = 0; i < n; ++i) f(i);
         return;

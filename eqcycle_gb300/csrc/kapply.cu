@@ -45,6 +45,7 @@ template <class T, int TEX, int TEY>
 __global__ void __launch_bounds__(256) k_apply(const T* __restrict__ x, T* __restrict__ y, ApplyArgs<T> A,
                                                T sign, int mode) {
     EQC_GRID_WAIT();
+    if (A.gate && *A.gate != A.gate_val) return;
     const Layout L = A.L;
     const bool strip = mode >= 2;
     const int ex0 = blockIdx.x * TEX;
@@ -268,6 +269,7 @@ template <class T, int TEX, int TEY, int NT>
 __global__ void __launch_bounds__(NT) k_apply_lines(const T* __restrict__ x, T* __restrict__ y, ApplyArgs<T> A,
                                                     T sign, int zero_row0) {
     EQC_GRID_WAIT();
+    if (A.gate && *A.gate != A.gate_val) return;
     const Layout L = A.L;
     constexpr int UX = 4 * TEX + 5, UY = 4 * TEY + 5;   // node tile incl. one halo element
     constexpr int OX = 4 * TEX, OY = 4 * TEY;           // owned nodes
@@ -356,6 +358,7 @@ __global__ void __launch_bounds__(NT) k_apply_tma(const __grid_constant__ CUtens
                                                   const __grid_constant__ CUtensorMap wmap, T* __restrict__ y,
                                                   ApplyArgs<T> A, T sign, int zero_row0) {
     EQC_GRID_WAIT();
+    if (A.gate && *A.gate != A.gate_val) return;
     constexpr int UY = 4 * TEY + 5;
     constexpr int OX = 4 * TEX, OY = 4 * TEY;
     constexpr int EX = TEX + 1, EY = TEY + 1;
@@ -414,6 +417,7 @@ __global__ void __launch_bounds__(NT) k_apply_pipe(const __grid_constant__ CUten
                                                    const __grid_constant__ CUtensorMap wmap, T* __restrict__ y,
                                                    ApplyArgs<T> A, T sign, int zero_row0, int ntx, int ntiles) {
     EQC_GRID_WAIT();
+    if (A.gate && *A.gate != A.gate_val) return;
     using PL = PipeLayout<T, TEX, TEY>;
     extern __shared__ __align__(128) unsigned char smem[];
     T* ys = reinterpret_cast<T*>(smem + PSTAGES * PL::STAGE);
@@ -630,13 +634,21 @@ template <int ROWS, int MINB>
 __global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const float* __restrict__ x, float* __restrict__ y,
                                                                      ApplyArgs<float> A, float sign, int zero_row0,
                                                                      OpEpi<float> E) {
-    EQC_GRID_WAIT();
     const Layout L = A.L;
     __shared__ float Ts[ROWS + 1][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int ex = (int)blockIdx.x * 31 - 1 + lane;
     const int ey = (int)blockIdx.y * ROWS - 1 + w;
     const bool real = ex >= 0 && ex < L.NelX && ey >= 0 && ey < L.NelY;
+    // the element data are constant (written only between launches, by the host): their loads
+    // are issued before the wait for the grids this launch depends on, so they overlap the
+    // predecessor's tail when the launch is programmatic
+    float4 wq[7];
+    const float4* wp = reinterpret_cast<const float4*>(A.Wp + ((int64_t)(real ? ey : 0) * L.NelX + (real ? ex : 0)) * 28);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) wq[k] = real ? __ldg(wp + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+    EQC_GRID_WAIT();
+    if (A.gate && *A.gate != A.gate_val) return;
 
     // every load of the lane is issued before the first use (one memory latency, not twelve)
     float4 v[5];
@@ -650,10 +662,6 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), MINB) k_apply_rows(const floa
         const int ix = 4 * ex + 4;
         n4s[j] = (lane == 31 && rowok && ix >= 0 && ix < L.nx) ? __ldg(x + (int64_t)iy * L.ld + ix) : 0.f;
     }
-    float4 wq[7];
-    const float4* wp = reinterpret_cast<const float4*>(A.Wp + ((int64_t)(real ? ey : 0) * L.NelX + (real ? ex : 0)) * 28);
-#pragma unroll
-    for (int k = 0; k < 7; ++k) wq[k] = real ? __ldg(wp + k) : make_float4(0.f, 0.f, 0.f, 0.f);
     float u[5][5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
@@ -730,7 +738,6 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
                                                                 const __grid_constant__ CUtensorMap wmap,
                                                                 float* __restrict__ y, ApplyArgs<float> A, float sign,
                                                                 int zero_row0, int nsx, int rw, OpEpi<float> E) {
-    EQC_GRID_WAIT();
     extern __shared__ __align__(128) unsigned char smem[];
     const Layout L = A.L;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -740,11 +747,18 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
     const int nt = (r_end - r0 + WK_ROWS) / WK_ROWS;  // tiles cover rows r0 - 1 .. r_end - 1
     float* Ts = reinterpret_cast<float*>(smem + WK_TS_OFF);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + WK_BAR_OFF);
-    auto issue = [&](int k) {
+    auto issue_w = [&](int k) {   // element records of tile k; the barrier expects the node rows too
         const int st = k & 1, base = r0 - 1 + WK_ROWS * k;
         mbar_expect_tx(&bar[st], (uint32_t)(WK_U_BYTES + WK_W_BYTES));
-        tma_load_2d(smem + st * WK_STAGE, &umap, &bar[st], 4 * (ex0 - 1), 4 * base);
         tma_load_3d(smem + st * WK_STAGE + WK_W_OFF, &wmap, &bar[st], 0, ex0 - 1, base);
+    };
+    auto issue_u = [&](int k) {   // node rows of tile k
+        const int st = k & 1, base = r0 - 1 + WK_ROWS * k;
+        tma_load_2d(smem + st * WK_STAGE, &umap, &bar[st], 4 * (ex0 - 1), 4 * base);
+    };
+    auto issue = [&](int k) {
+        issue_w(k);
+        issue_u(k);
     };
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -752,7 +766,20 @@ __global__ void __launch_bounds__(32 * WK_ROWS, 2) k_apply_walk(const __grid_con
         mbar_fence_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0) issue(0);   // the first tile alone: it reaches every CTA before any second one
+    // the element data are constant (written only between launches, by the host): the first
+    // tile's records are requested before the wait for the grids this launch depends on, so they
+    // stream in during the predecessor's tail when the launch is programmatic; the node rows (the
+    // predecessor's output) after it.  The first tile alone: it reaches every CTA before any
+    // second one.
+    // A gated launch (A.gate) requests nothing before the wait: it may have no work.
+    const bool gated = A.gate != nullptr;
+    if (threadIdx.x == 0 && !gated) issue_w(0);
+    EQC_GRID_WAIT();
+    if (gated && *A.gate != A.gate_val) return;
+    if (threadIdx.x == 0) {
+        if (gated) issue_w(0);
+        issue_u(0);
+    }
     const int ex = ex0 - 1 + lane;
     for (int k = 0; k < nt; ++k) {
         const int st = k & 1;
@@ -1103,6 +1130,16 @@ void apply_K(const T* x, T* y, const ApplyArgs<T>& A, T sign, int mode, cudaStre
     k_apply<T, TEX, TEY><<<grid, 256, sm, s>>>(x, y, A, sign, mode);
     EQC_CHECK_LAUNCH();
     count_launch();
+}
+
+bool apply_K_fault32(const float* x, float* y, const ApplyArgs<float>& A, cudaStream_t s) {
+    if (!A.Wp || !aligned16(x) || !aligned16(y)) return false;
+    // one element row per CTA (warp 0 the virtual row below the fault, W = 0), grid row 0 only
+    const dim3 g((A.L.NelX + 1 + 30) / 31, 1);
+    k_apply_rows<1, 8><<<g, 64, 0, s>>>(x, y, A, 1.0f, 0, OpEpi<float>());
+    EQC_CHECK_LAUNCH();
+    count_launch();
+    return true;
 }
 
 bool apply_K_epi(const float* x, const ApplyArgs<float>& A, int mode, const OpEpi<float>& E, cudaStream_t s) {

@@ -285,7 +285,7 @@ std::vector<double> dense_inverse_spd(const std::vector<double>& A9, int cx, int
         for (int c0 = 0; c0 < n; c0 += TB)
             for (int i = i0; i < i1; ++i)
                 for (int c = c0; c < std::min(n, c0 + TB); ++c) Inv[(size_t)i * n + c] = T[(size_t)c * n + i];
-    });
+    }, 1);
     return Inv;
 }
 

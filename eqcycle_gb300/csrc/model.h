@@ -48,6 +48,7 @@ struct Ctrl {
     // mixed-precision Newmark: Kd = K d kept in FP64, updated by the FP32 apply of each step's
     // increment and refreshed in FP64 at the start of a dynamic phase and every KD_REFRESH steps
     int kd_valid, kd_age, kd_full;
+    double dt_step;        // dt of the dynamic step in progress (the mixed method's split predictor)
 };
 constexpr int KD_REFRESH = 256;
 
@@ -123,6 +124,20 @@ struct Handle {
     DBuf<double> bcL, bcT;
     int nBcNodes = 0;
     bool creep_prefix = false;   // iCreep lies in the fault row (its nodes: the prefix [0, NFBC0))
+    // the mixed method's dynamic step in four kernels: absorbing-boundary coefficients by position
+    // on the two edges the lists lie on (column ix = 0: iBcL; row iy = ny - 1: iBcT)
+    DBuf<double> edgeL, edgeT;
+    DBuf<int> edgeLhas, edgeThas;
+    bool nm_fused = false;       // the lists lie on those edges, once each, and creep_prefix
+    int edgeL0has = 0;           // the fault's bottom node (0, 0) is in iBcL, with coefficient
+    double edgeL0 = 0.0;
+    DBuf<unsigned> fault_count;  // CTAs of k_dyn_fault_nm done (its last one runs the control)
+    DBuf<double> fault_part;     // their partial reductions (three doubles' room each)
+    // the fault row of that step runs on a second stream beside the other rows, the FP64
+    // recomputation of K d (refresh steps) on a third beside the FP32 apply of the increment
+    cudaStream_t side_stream = nullptr, side_stream2 = nullptr;
+    bool pdl_off = false;        // the graph being captured holds that step: no programmatic edges
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
     DBuf<int64_t> d_ref2lay;
     // element data
     DBuf<double> W64, W64p;
@@ -198,6 +213,10 @@ void tma_init_for(TmaCache& c, const Layout& L, const float* W32p, const double*
 // FP32 apply y = K x (mode 0/1 as apply_K) whose owned nodes are finished by the epilogue E
 // (residual or Chebyshev step) instead of stored; false when the selected kernel has none.
 bool apply_K_epi(const float* x, const ApplyArgs<float>& A, int mode, const OpEpi<float>& E, cudaStream_t s);
+// y = K x (FP32) on the node rows 0..3 of the fault's element row, by the element-per-lane
+// arithmetic of the full FP32 applies (variants 0 and 4-8): row 0 has the bits of their row 0.
+// False when the padded element data or 16-byte aligned vectors are missing.
+bool apply_K_fault32(const float* x, float* y, const ApplyArgs<float>& A, cudaStream_t s);
 
 // blas.cu
 void dot64(Handle& h, const double* x, const double* y, int64_t n, double* out_dev);

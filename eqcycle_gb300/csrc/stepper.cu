@@ -13,6 +13,7 @@
 #include "fault.cuh"
 #include "reduce.cuh"
 #include "vec.cuh"
+#include "df.cuh"
 #include <cmath>
 #include <algorithm>
 #include <chrono>
@@ -192,6 +193,73 @@ __global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d,
 }
 
 
+// The mixed method's predictor with the step counter of main.jl:221-222 (it += 1, t += dt)
+// folded in: vPre on the fault, v += dt/2 a, then d += dt v with that v (dt v + dt^2/2 a as one
+// product), and the FP32 increment dd32 = dt v for the FP32 apply.  Two FP64 operations per
+// node (GB300's FP64 rate bounds these vector kernels); the conversion to FP32 uses integer
+// operations.  The step runs as two launches over [i0, n): the node rows of the first element
+// row (lead = 1: the step's bookkeeping -- it, t, the choice how the step gets K d -- after which
+// the fault row's work can start), then the rest (lead = 0: the step's dt is read from dt_step,
+// since the control at the end of the fault row's work may already have replaced dt with the
+// next step's).
+__global__ void __launch_bounds__(256) k_dyn_predict_nm(double* __restrict__ d, double* __restrict__ v,
+                                                        const double* __restrict__ a, double* __restrict__ vPre_f,
+                                                        float* __restrict__ dd32, int Nf, int64_t i0, int64_t n,
+                                                        Ctrl* C, int lead) {
+    EQC_GRID_WAIT();
+    const double dt = lead ? C->dt : C->dt_step, hdt = C->half_dt;
+    const float dt_hi = __double2float_rn(dt), dt_lo = __double2float_rn(dt - (double)dt_hi);
+    if (lead && blockIdx.x == 0 && threadIdx.x == 0) {
+        C->dt_step = dt;
+        C->it += 1;
+        C->t = C->t + dt;
+        C->r_valid = 0;
+        C->qs_prev = 0;
+        const int full = (!C->kd_valid || C->kd_age >= KD_REFRESH) ? 1 : 0;
+        C->kd_full = full;
+        C->kd_valid = 1;
+        C->kd_age = full ? 0 : C->kd_age + 1;
+    }
+    for (int64_t i = i0 + 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n;
+         i += 4 * (int64_t)gridDim.x * blockDim.x) {
+        double dd4[4], vv[4], aa[4];
+        float f[4];
+        ld4(d + i, dd4);
+        ld4(v + i, vv);
+        ld4(a + i, aa);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i + k < Nf) vPre_f[i + k] = vv[k];
+            const double vh = __fma_rn(hdt, aa[k], vv[k]);
+            dd4[k] = __fma_rn(dt, vh, dd4[k]);
+            f[k] = nm_incr32(vh, dt_hi, dt_lo);
+            vv[k] = vh;
+        }
+        st4(d + i, dd4);
+        st4(v + i, vv);
+        st4(dd32 + i, f);
+    }
+}
+
+// The end of the mixed Newmark step (NmEpi) on every real node off the fault row: K d += K dd
+// (t32, the FP32 apply of the step's increment, unless K d was just recomputed in FP64),
+// a = -K d with the absorbing terms, a *= 1/M, v += dt/2 a.
+__global__ void __launch_bounds__(256) k_dyn_finish(NmEpi N, const float* __restrict__ t32) {
+    EQC_GRID_WAIT();
+    const double hdt = *N.hdt;
+    if (*N.kd_full) t32 = nullptr;
+    const int gx = N.ld / 4;
+    const int64_t ng = (int64_t)gx * N.ny;   // groups of 4 nodes; row 0 is the fault kernel's
+    for (int64_t g = gx + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
+        const int iy = (int)(g / gx), ix0 = 4 * (int)(g - (int64_t)iy * gx);
+        if (ix0 >= N.nx) continue;
+        const int64_t off = (int64_t)iy * N.ld + ix0;
+        float t[4] = {0.f, 0.f, 0.f, 0.f};
+        if (t32) ld4(t32 + off, t);
+        newmark4(N, off, ix0, iy, t, t32 != nullptr, hdt);
+    }
+}
+
 // a = -K d with K d either refreshed (Kd written by the FP64 apply) or Kd += K dd (t32, FP32).
 __global__ void __launch_bounds__(256) k_dyn_force(double* __restrict__ Kd, const float* __restrict__ t32,
                                                    double* __restrict__ a, int64_t n, Ctrl* C) {
@@ -315,72 +383,173 @@ __global__ void __launch_bounds__(256) k_dyn_correct_inv(double* __restrict__ a,
 
 // ---------------------------------------------------------------- control
 // Vfmax (main.jl:348), hypocentre argmax (main.jl:367), regime switch (main.jl:439-443),
-// next dt (dtevol!, src/dtevol.jl:5-44).  One CTA.
-__global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, FaultArgs f, Ctrl* C) {
-    EQC_GRID_WAIT();
-    __shared__ double smax[FT / 32];
-    __shared__ int sidx[FT / 32];
-    __shared__ double smin[FT / 32];
-    __shared__ int s_next;
-    const double Vpl = C->Vpl;
-    const double dtmax = 50.0 * 24 * 60 * 60;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // Vfmax and its first index, the regime of the next step
-    double vmax = -INFINITY;
-    int imax = 0x7fffffff;
-    int nan = 0;   // Julia's maximum propagates NaN: so does Vfmax here
-    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) {
-        const double vk = v[k];
-        if (vk > vmax) { vmax = vk; imax = k; }
-        if (vk != vk) nan = 1;
+// next dt (dtevol!, src/dtevol.jl:5-44).  The reductions are a maximum with its first index
+// and a minimum, so their value does not depend on how the nodes are grouped: one CTA of any
+// size (k_control), or per-CTA partials combined by the last CTA of the dynamic fault kernel.
+struct CtlAcc {
+    double vmax;   // largest v over the fault (NaN flagged apart: Julia's maximum propagates it)
+    int imax;      // its first index
+    int nan;
+    double dmin;   // dtevol!: min over the friction nodes of XiLf / |V| where |V| dtmax > XiLf
+};
+static_assert(sizeof(CtlAcc) == 3 * sizeof(double), "the fault kernel's partials take three doubles each");
+static_assert(FNT == 32, "the dynamic fault kernel reduces with one warp per CTA");
+constexpr double DTMAX = 50.0 * 24 * 60 * 60;   // src/dtevol.jl:7
+__device__ __forceinline__ CtlAcc ctl_init() { return CtlAcc{-INFINITY, 0x7fffffff, 0, DTMAX}; }
+__device__ __forceinline__ void ctl_add(CtlAcc& c, int k, double vk, const FaultArgs& f, double Vpl) {
+    if (vk > c.vmax) { c.vmax = vk; c.imax = k; }
+    if (vk != vk) c.nan = 1;
+    if (k >= f.NFBC0) {
+        const double sr = fabs(2 * vk + Vpl);
+        if (sr * DTMAX > f.XiLf[k]) c.dmin = fmin(c.dmin, f.XiLf[k] / sr);
     }
+}
+__device__ __forceinline__ void ctl_merge(CtlAcc& c, const CtlAcc& o) {
+    if (o.vmax > c.vmax || (o.vmax == c.vmax && o.imax < c.imax)) { c.vmax = o.vmax; c.imax = o.imax; }
+    c.nan |= o.nan;
+    c.dmin = fmin(c.dmin, o.dmin);
+}
+__device__ __forceinline__ CtlAcc ctl_warp(CtlAcc c) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const double ov = __shfl_down_sync(0xffffffffu, vmax, o);
-        const int oi = __shfl_down_sync(0xffffffffu, imax, o);
-        if (ov > vmax || (ov == vmax && oi < imax)) { vmax = ov; imax = oi; }
+        CtlAcc x;
+        x.vmax = __shfl_down_sync(0xffffffffu, c.vmax, o);
+        x.imax = __shfl_down_sync(0xffffffffu, c.imax, o);
+        x.nan = __shfl_down_sync(0xffffffffu, c.nan, o);
+        x.dmin = __shfl_down_sync(0xffffffffu, c.dmin, o);
+        ctl_merge(c, x);
     }
-    if (lane == 0) { smax[w] = vmax; sidx[w] = imax; }
-    const int anynan = __syncthreads_or(nan);
-    if (threadIdx.x == 0) {
-        double bv = -INFINITY;
-        int bi = 0x7fffffff;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q)
-            if (smax[q] > bv || (smax[q] == bv && sidx[q] < bi)) { bv = smax[q]; bi = sidx[q]; }
-        if (anynan) { bv = __longlong_as_double(0x7ff8000000000000LL); bi = 0; }
-        const double Vfmax = 2 * bv + Vpl;
-        C->Vfmax = Vfmax;
-        C->vhypo = Vfmax;
-        C->ihypo = bi;
-        const int iso = C->isolver;
-        const int next = ((iso == 1 && Vfmax < 5e-3) || (iso == 2 && Vfmax < 2e-3)) ? 1 : 2;
-        C->isolver = next;
-        C->dt_prev = C->dt;
-        if (iso == 1) C->qs_prev = 1;
-        s_next = next;
-        if (next == 2) C->dt = C->dtmin;   // dtevol!: the dynamic step takes dtmin
-    }
-    __syncthreads();
-    if (s_next != 1) return;
-    // dtevol! for a quasi-static next step: min over XiLf / |V|, capped at 1.2 dt
-    double dmin = dtmax;
-    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) {
-        if (k >= f.NFBC0) {
-            const double sr = fabs(2 * v[k] + Vpl);
-            if (sr * dtmax > f.XiLf[k]) dmin = fmin(dmin, f.XiLf[k] / sr);
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_down_sync(0xffffffffu, dmin, o));
-    if (lane == 0) smin[w] = dmin;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double bm = dtmax;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) bm = fmin(bm, smin[q]);
-        double dtnx = bm;
+    return c;
+}
+// The decision of the step (one thread): Vfmax, hypocentre, next regime, next dt.
+__device__ __forceinline__ void ctl_finish(const CtlAcc& c, Ctrl* C) {
+    const double bv = c.nan ? __longlong_as_double(0x7ff8000000000000LL) : c.vmax;
+    const double Vfmax = 2 * bv + C->Vpl;
+    C->Vfmax = Vfmax;
+    C->vhypo = Vfmax;
+    C->ihypo = c.nan ? 0 : c.imax;
+    const int iso = C->isolver;
+    const int next = ((iso == 1 && Vfmax < 5e-3) || (iso == 2 && Vfmax < 2e-3)) ? 1 : 2;
+    C->isolver = next;
+    C->dt_prev = C->dt;
+    if (iso == 1) C->qs_prev = 1;
+    if (next == 2) {
+        C->dt = C->dtmin;   // dtevol!: the dynamic step takes dtmin
+    } else {                // a quasi-static next step: min over XiLf / |V|, capped at 1.2 dt
+        double dtnx = c.dmin;
         if (C->dtmin > dtnx) dtnx = C->dtmin;
         if (dtnx > 1.2 * C->dt_prev) dtnx = 1.2 * C->dt_prev;
         C->dt = dtnx;
+    }
+}
+
+// One CTA (up to 1024 threads) over the fault row.
+__global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, FaultArgs f, Ctrl* C) {
+    EQC_GRID_WAIT();
+    __shared__ CtlAcc sh[32];
+    const double Vpl = C->Vpl;
+    CtlAcc c = ctl_init();
+    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) ctl_add(c, k, v[k], f, Vpl);
+    c = ctl_warp(c);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        CtlAcc t = sh[0];
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) ctl_merge(t, sh[q]);
+        ctl_finish(t, C);
+    }
+}
+
+// The fault row of the mixed method's dynamic step, from a = -(K d)[iFlt] (t0, the FP64 strip
+// apply of the predicted displacement, on the steps that refresh K d; else K d += q0) to the end
+// of the step, then the control of k_control: the creeping nodes' a = 0 and the absorbing term
+// of the fault's bottom node (main.jl:314-318), the friction Newton solves (warm-started,
+// dev_NR_warm) and a[iFlt] -= FltB tau (main.jl:321-331), a *= 1/M, v += dt/2 a,
+// creeping nodes a = v = 0 (main.jl:336-344); the last CTA to finish (counted in *count, which
+// it clears again) combines the per-CTA partials in part[], reduces Vfmax, switches the regime and
+// takes the next dt.  It runs beside the end of the step on the other rows, which it shares no
+// node with.  One warp (FNT threads) per CTA.
+__global__ void __launch_bounds__(FNT) k_dyn_fault_nm(double* __restrict__ a, double* __restrict__ v,
+                                                      const double* __restrict__ t0, const float* __restrict__ q0,
+                                                      double* __restrict__ Kd, FaultArgs f, Ctrl* C,
+                                                      const double* __restrict__ invM, int hasL0, double cL0,
+                                                      CtlAcc* part, unsigned* count) {
+    EQC_GRID_WAIT();
+    __shared__ bool last;
+    const double dt = C->dt_step, hdt = C->half_dt, Vpl = C->Vpl;
+    const int full = C->kd_full;
+    CtlAcc acc = ctl_init();
+    for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
+        const double vk0 = v[k];
+        // K d on the fault row as on the other rows: recomputed in FP64 (t0) on the steps that
+        // refresh it (the full FP64 apply beside this kernel stores it), else K d += K dd (q0, the
+        // FP32 apply of the increment on the fault's element row, whose row 0 has the bits of the
+        // full FP32 apply's: every row's K d then carries the same FP32 rounding.  A strip kernel
+        // with another summation order let the fault row's K d drift from its neighbours', a net
+        // force that made the displacement error ten times larger after 300 steps.)
+        double kd;
+        if (full) {
+            kd = t0[k];
+        } else {
+            kd = __dadd_rn(Kd[k], f32_to_f64(q0[k]));
+            Kd[k] = kd;
+        }
+        double a0 = -kd;
+        if (f.bcflag[k]) a0 = 0.0;
+        if (k == 0 && hasL0) a0 = a0 - cL0 * vk0;
+        const double vfree = 2 * vk0 + 2 * hdt * a0 / f.Mf[k];
+        f.FltVfree[k] = vfree;
+        const double vf = 2 * f.vPre[k] + Vpl;
+        f.Vf[k] = vf;
+        if (k >= f.NFBC0) {
+            const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, vf, 1e-5);
+            f.psi1[k] = p1;
+            double V1, T1;
+            // the first search starts from the node's current shear stress (tau + tauo)
+            dev_NR_warm(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], f.tau[k] + f.tauo[k], f.tauo[k], p1, f.FltZ[k],
+                        vfree, &V1, &T1);
+            f.Vf1[k] = V1;
+            f.tau1[k] = T1;
+            if (vf > 1e10 || isnan(vf) || isnan(T1)) atomicMin(&C->fail, k + 1);
+            const double p2 = dev_IDS2(f.xLf[k], f.Vo[k], f.psi[k], p1, dt, vf, V1);
+            f.psi2[k] = p2;
+            double V2, T2;
+            dev_NR_warm(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], T1, f.tauo[k], p2, f.FltZ[k], vfree, &V2, &T2);
+            f.Vf2[k] = V2;
+            f.tau2[k] = T2;
+        }
+        double t = f.tau2[k] - f.tauo[k];
+        if (f.creep[k]) t = 0.;
+        f.tau[k] = t;
+        f.psi[k] = f.psi2[k];
+        double am = __dmul_rn(a0 - f.FltB[k] * t, invM[k]), vk = __fma_rn(hdt, am, vk0);
+        if (f.creep[k]) am = vk = 0.0;
+        a[k] = am;
+        v[k] = vk;
+        ctl_add(acc, k, vk, f, Vpl);
+    }
+    acc = ctl_warp(acc);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = acc;
+        __threadfence();
+        last = atomicAdd(count, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    CtlAcc c = ctl_init();
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+        CtlAcc o;
+        o.vmax = __ldcg(&part[q].vmax);
+        o.imax = __ldcg(&part[q].imax);
+        o.nan = __ldcg(&part[q].nan);
+        o.dmin = __ldcg(&part[q].dmin);
+        ctl_merge(c, o);
+    }
+    c = ctl_warp(c);
+    if (threadIdx.x == 0) {
+        ctl_finish(c, C);
+        *count = 0u;
     }
 }
 
@@ -671,10 +840,90 @@ static void enqueue_qs(Handle& h, bool graph) {
 }
 
 // Dynamic step (main.jl:297-345): Newmark predictor, K d, boundaries, fault, corrector.
+static NmEpi nm_args(Handle& h) {
+    NmEpi N;
+    N.Kd = h.Kd.p;
+    N.v = h.v.p;
+    N.a = h.a.p;
+    N.invM = h.invM.p;
+    N.cL = h.edgeL.p;
+    N.cT = h.edgeT.p;
+    N.hasL = h.edgeLhas.p;
+    N.hasT = h.edgeThas.p;
+    N.hdt = &h.ctrl.p->half_dt;
+    N.kd_full = &h.ctrl.p->kd_full;
+    N.ld = h.L.ld;
+    N.nx = h.L.nx;
+    N.ny = h.L.ny;
+    return N;
+}
+
+// The mixed method's dynamic step, on three streams:
+//   main:  predictor of the first element row's node rows (the step's bookkeeping) -> predictor
+//          of the other rows -> FP32 apply of the increment -> end of the step off the fault row
+//          (k_dyn_finish: K d += K dd, boundary terms, a /= M, v += dt/2 a);
+//   side:  the apply of the fault's element row (FP32 of the increment, or FP64 of d on the
+//          steps that refresh K d) -> the fault kernel, which ends the step on the fault row and
+//          runs the control;
+//   side2: on the steps that refresh K d, the FP64 apply of d (forked after the predictor).
+// At the start of a dynamic phase and every KD_REFRESH steps K d is recomputed in FP64.  The
+// lead predictor's choice reaches the applies through gates (ApplyArgs::gate) rather than
+// conditional graph nodes, so the step is the same straight sequence of launches eagerly and in
+// a graph.  The step graphs keep ordinary edges here (no programmatic launches): a dependent
+// launched early parks its CTAs on the SMs while it waits, and those slots are what the other
+// streams' kernels need (measured on dz480: 70 us per step without, 87 us with).
+static void enqueue_dyn_mixed_fused(Handle& h) {
+    cudaStream_t s = h.stream;
+    if (h.capturing) h.pdl_off = true;
+    const int64_t n = h.L.size();
+    const int* full = &h.ctrl.p->kd_full;
+    auto gated = [&](auto A, int val) {
+        A.gate = full;
+        A.gate_val = val;
+        return A;
+    };
+    const int64_t n0 = std::min<int64_t>(5 * (int64_t)h.L.ld, n);
+    k_dyn_predict_nm<<<vblocks4(n0), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, 0, n0, h.ctrl.p, 1);
+    EQC_CHECK_LAUNCH();
+    EQC_CUDA(cudaEventRecord(h.ev_fork, s));
+    // fault row
+    EQC_CUDA(cudaStreamWaitEvent(h.side_stream, h.ev_fork, 0));
+    const ApplyArgs<float> a32f = gated(args32(h), 0);
+    if (!apply_K_fault32(h.g32.p, h.z32.p, a32f, h.side_stream))
+        apply_K<float>(h.g32.p, h.z32.p, a32f, 1.0f, 3, h.side_stream);
+    apply_K<double>(h.d.p, h.tmp64c.p, gated(args64(h), 1), 1.0, 3, h.side_stream);
+    k_dyn_fault_nm<<<fblocks(h.F.Nf), FNT, 0, h.side_stream>>>(h.a.p, h.v.p, h.tmp64c.p, h.z32.p, h.Kd.p,
+                                                               fargs(h, h.bcflag.p), h.ctrl.p,
+                                                               h.invM.p, h.edgeL0has, h.edgeL0,
+                                                               reinterpret_cast<CtlAcc*>(h.fault_part.p),
+                                                               h.fault_count.p);
+    EQC_CHECK_LAUNCH();
+    EQC_CUDA(cudaEventRecord(h.ev_join, h.side_stream));
+    // K d off the fault row
+    k_dyn_predict_nm<<<vblocks4(n - n0), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n0, n,
+                                                      h.ctrl.p, 0);
+    EQC_CHECK_LAUNCH();
+    EQC_CUDA(cudaEventRecord(h.ev_fork2, s));
+    EQC_CUDA(cudaStreamWaitEvent(h.side_stream2, h.ev_fork2, 0));
+    apply_K<double>(h.d.p, h.Kd.p, gated(args64(h), 1), 1.0, 0, h.side_stream2);
+    EQC_CUDA(cudaEventRecord(h.ev_join2, h.side_stream2));
+    apply_K<float>(h.g32.p, h.q32.p, gated(args32(h), 0), 1.0f, 0, s);
+    EQC_CUDA(cudaStreamWaitEvent(s, h.ev_join2, 0));
+    k_dyn_finish<<<vblocks(n / 4), 256, 0, s>>>(nm_args(h), h.q32.p);
+    EQC_CHECK_LAUNCH();
+    count_launch(4);
+    EQC_CUDA(cudaStreamWaitEvent(s, h.ev_join, 0));
+    launch_check();
+}
+
 static void enqueue_dyn(Handle& h, bool graph) {
     cudaStream_t s = h.stream;
     const int64_t n = h.L.size();
     FaultArgs f = fargs(h, h.bcflag.p);
+    if (h.opt.precision == EQC_MIXED && h.nm_fused) {
+        enqueue_dyn_mixed_fused(h);
+        return;
+    }
     if (h.opt.precision == EQC_MIXED) {
         // FP64 accumulation of d and of K d, FP32 apply of the step's increment
         if (graph) {
@@ -733,13 +982,20 @@ static void enqueue_dyn(Handle& h, bool graph) {
 
 // One whole time step, ending with the control kernel (Vfmax, regime, next dt).
 void enqueue_step(Handle& h, int iso, bool graph) {
-    k_step_begin<<<1, 1, 0, h.stream>>>(h.ctrl.p);
-    count_launch();
+    // the mixed method's dynamic step advances it and t in its predictor and runs the control in
+    // its fault kernel
+    const bool fused = iso == 2 && h.opt.precision == EQC_MIXED && h.nm_fused;
+    if (!fused) {
+        k_step_begin<<<1, 1, 0, h.stream>>>(h.ctrl.p);
+        count_launch();
+    }
     if (iso == 1) enqueue_qs(h, graph);
     else enqueue_dyn(h, graph);
-    k_control<<<1, FT, 0, h.stream>>>(h.v.p, fargs(h, h.bcflag.p), h.ctrl.p);
-    launch_check();
-    count_launch();
+    if (!fused) {
+        k_control<<<1, FT, 0, h.stream>>>(h.v.p, fargs(h, h.bcflag.p), h.ctrl.p);
+        launch_check();
+        count_launch();
+    }
 }
 
 void destroy_graphs(Handle& h) {
@@ -808,6 +1064,7 @@ static StepGraph& batched_graph(Handle& h, int iso) {
     h.capturing = &G;
     capture_counting(true);
     try {
+        h.pdl_off = false;
         EQC_CUDA(cudaStreamBeginCapture(h.stream, cudaStreamCaptureModeThreadLocal));
         const cudaGraphConditionalHandle hw = cond_handle(h, 1);   // the first step always runs
         cond_begin(h, cudaGraphCondTypeWhile, hw);
@@ -818,7 +1075,8 @@ static StepGraph& batched_graph(Handle& h, int iso) {
         count_launch();
         cond_end(h);
         EQC_CUDA(cudaStreamEndCapture(h.stream, &G.graph));
-        h.pdl_edges += make_programmatic(G.graph);
+        if (!h.pdl_off) h.pdl_edges += make_programmatic(G.graph);
+        h.pdl_off = false;
     } catch (...) {
         abort_capture(h);
         h.capturing = nullptr;
@@ -839,10 +1097,12 @@ static StepGraph& step_graph(Handle& h, int iso) {
     h.capturing = &G;
     capture_counting(true);
     try {
+        h.pdl_off = false;
         EQC_CUDA(cudaStreamBeginCapture(h.stream, cudaStreamCaptureModeThreadLocal));
         enqueue_step(h, iso, true);
         EQC_CUDA(cudaStreamEndCapture(h.stream, &G.graph));
-        h.pdl_edges += make_programmatic(G.graph);
+        if (!h.pdl_off) h.pdl_edges += make_programmatic(G.graph);
+        h.pdl_off = false;
     } catch (...) {
         abort_capture(h);
         h.capturing = nullptr;

@@ -323,7 +323,8 @@ eqc_status eqc_time_apply(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t fl
 /* Time nrep back-to-back launches of the stiffness apply rotating over ncopies replicas of its
  * whole working set (x, y, W), so that with replicas larger than L2 together every launch
  * streams its data from HBM; *ms gets the mean launch duration (CUDA events around the
- * batch, on the handle's stream). */
+ * batch, on the handle's stream).  The batch is one CUDA graph whose consecutive launches are
+ * programmatic dependent launches, as the library's step graphs run their kernels. */
 eqc_status eqc_time_apply_stream(eqc_handle* h, int32_t dtype, int32_t nrep, int32_t ncopies, double* ms);
 
 /* Solver autotuner (no counterpart in the reference): times `reps` graph-replayed trial

@@ -395,10 +395,21 @@ void AMG::precond(double* x, const double* b) {
     vcycle(0, x, b);
 }
 
+// Partial sums over fixed blocks of 4096 entries, added in block order: the same bits for any
+// thread count and any run (an OpenMP reduction combines the threads' sums in arrival order).
 static double dot(int64_t n, const double* a, const double* b) {
+    constexpr int64_t BS = 4096;
+    const int64_t nb = (n + BS - 1) / BS;
+    vec part(nb, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < nb; ++q) {
+        double s = 0.0;
+        const int64_t e = std::min(n, (q + 1) * BS);
+        for (int64_t i = q * BS; i < e; ++i) s += a[i] * b[i];
+        part[q] = s;
+    }
     double s = 0.0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-    for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+    for (int64_t q = 0; q < nb; ++q) s += part[q];
     return s;
 }
 

@@ -106,3 +106,43 @@ def test_double_float_apply_matches_fp64(eqclib, name):
         xs[:, :nx] = 0.3 + 1e-3 * ix + 2e-3 * iy + 1e-4 * torch.sin(0.05 * ix) * torch.cos(0.03 * iy)
         z64, zdf = _apply(s, torch, xs, 0), _apply(s, torch, xs, 2)
         assert np.max(np.abs(zdf - z64)) <= 1e-12 * scale * float(xs.abs().max()) / 0.5
+
+
+@pytest.mark.parametrize("variant", [0, 8])
+def test_mixed_newmark_step_variants(eqclib, monkeypatch, variant):
+    """The mixed method's dynamic step in its four-kernel form (predictor with the step counter;
+    FP32 apply of the increment and one vector kernel ending the step off the fault row; the
+    fault row -- its element row's apply, friction, end of step and control -- on a second stream
+    beside them) replayed from its CUDA graph gives the same bits as the same kernels launched one
+    by one, through 300 steps of fast slip that include a refresh of K d in FP64.  Against the
+    plain FP64 step its error in every field stays within 1.5 times that of the seven-kernel form
+    (EQC_NO_NM_FUSE: predictor, apply, force, boundary, fault, correction and control kernels) plus
+    1e-7 of the field's scale.  This bound decides: a fault-row apply whose FP32 rounding differed
+    from the bulk apply's made the displacement error ten times that of the seven-kernel form."""
+    from eqcycle_gb300 import EQC_FP64, EQC_MIXED, EQC_PC_AMG
+    cfg = preset("dz40").replace(V_init=5e-2)
+    P = set_parameters(cfg)
+    fields = ("d", "v", "a", "psi", "tau")
+    out = []
+    for env, graphs, prec in ((None, 1, EQC_MIXED), (None, 0, EQC_MIXED), ("EQC_NO_NM_FUSE", 1, EQC_MIXED),
+                              (None, 1, EQC_FP64)):
+        monkeypatch.delenv("EQC_NO_NM_FUSE", raising=False)
+        if env:
+            monkeypatch.setenv(env, "1")
+        with Solver(P, precision=prec, precond=EQC_PC_AMG, apply_variant=variant, use_graphs=graphs) as s:
+            s.init(cfg.V_init)
+            st = s.run(300)                       # 300 > 256: one refresh of K d inside the phase
+            out.append((st["dyn_steps"], {k: s.state(k) for k in fields}, s.results().Vfmax))
+    assert out[0][0] >= 270, out[0][0]
+    assert np.array_equal(out[0][2], out[1][2])
+    ref = out[3][1]
+    errs = {}
+    for k in fields:
+        assert np.array_equal(out[0][1][k], out[1][1][k]), k
+        scale = np.max(np.abs(ref[k]))
+        errs[k] = (float(np.max(np.abs(out[0][1][k] - ref[k])) / scale),
+                   float(np.max(np.abs(out[2][1][k] - ref[k])) / scale))
+    print({k: f"{a:.2e} / {b:.2e}" for k, (a, b) in errs.items()})
+    for k, (fused, seven) in errs.items():
+        assert seven <= 1e-3, (k, seven)
+        assert fused <= 1.5 * seven + 1e-7, (k, fused, seven)

@@ -2,7 +2,11 @@
 the stiffness apply (1e-12), a quasi-static solve (1e-10), the first 40 quasi-static and 60
 dynamic steps (1e-8 / 1e-6, as the live oracle comparisons), and the event catalogue of the
 48 x 48 element model over 300 years, plain FP64 and mixed precision each within 2 % of the
-oracle's reference-mode catalogue (recurrence interval, coseismic slip, hypocentre depth)."""
+oracle's reference-mode catalogue (recurrence interval, coseismic slip, hypocentre depth), and
+every field of that run's results record (main.jl:479-498) against the oracle's
+(tests/golden/catalogue_homog48.npz): event times to 1e-3, hypocentres to two node spacings, the
+per-event stress and slip profiles, the 5-year snapshots of slip and stress (and of the slip rate
+before the first event) and every 5th coseismic snapshot to 2 % of each field's largest entry."""
 import importlib.util
 import os
 
@@ -84,3 +88,26 @@ def test_event_catalogue_within_two_percent_of_the_oracle(eqclib, gold, precisio
     for k in ("recurrence", "coseismic_slip", "hypocentre_depth"):
         assert c[k] <= 0.02, (k, c)
     assert np.max(np.abs(cat.Mw - ref.Mw)) <= 0.02
+    # every field of the results record against the oracle's 300-year run (catalogue_homog48.npz)
+    full = dict(np.load(os.path.join(HERE, "catalogue_homog48.npz")))
+    assert np.max(np.abs(res.tStart - full["tStart"]) / full["tStart"]) <= 1e-3
+    assert np.max(np.abs(res.tEnd - full["tEnd"]) / full["tEnd"]) <= 1e-3
+    assert np.max(np.abs(res.hypo - full["hypo"])) <= 250.0           # two GLL node spacings
+    errs = {}
+    for f in ("taubefore", "tauafter", "delfafter", "is_slip", "is_stress"):
+        a, b = getattr(res, f), full[f].astype(np.float64)
+        assert a.shape == b.shape, (f, a.shape, b.shape)
+        errs[f] = rel(a, b)
+    # the 5-year snapshots of the slip rate before the first event (after it, the slip rate of the
+    # slowly creeping parts depends on the exact timing of the rupture: only the event statistics
+    # are compared there)
+    pre = int(full["tStart"][0] // (5 * YR2SEC))
+    errs["is_slipvel before the first event"] = rel(res.is_slipvel[:, :pre],
+                                                    full["is_slipvel"][:, :pre].astype(np.float64))
+    assert res.seismic_slip.shape[1] == int(full["seismic_count"][0])
+    for f in ("seismic_slip", "seismic_slipvel", "seismic_stress"):
+        a, b = getattr(res, f)[:, ::5], full[f + "_every5"].astype(np.float64)
+        assert a.shape == b.shape, f
+        errs[f] = rel(a, b)
+    print(precision, {k: f"{v:.2e}" for k, v in errs.items()})
+    assert all(v <= 0.02 for v in errs.values()), errs
