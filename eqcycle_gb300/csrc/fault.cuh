@@ -58,16 +58,20 @@ __device__ __forceinline__ int dev_NR(double fo, double Vo, double cca, double c
     return 0;
 }
 
-// The mixed method's Newton search: NRsearch!'s iteration, stopping rule and failure statuses,
-// with the loop's constants hoisted (fa = s tau, Vf' = vp (help1 + help2), the right-hand side
-// FltZ FltVfree + tauo summed once) and explicit fused multiply-adds.  The caller starts it from
+// The mixed method's Newton search: NRsearch!'s iteration (src/NRsearch_serial.jl:47-98),
+// stopping rule and failure statuses, with the loop's constants hoisted (fa = s tau,
+// Vf' = vp (help1 + help2), the right-hand side FltZ FltVfree + tauo summed once) and explicit
+// fused multiply-adds.  The caller starts it from
 // the node's current shear stress instead of 0: the function tau -> tauo + FltZ (FltVfree - Vf(tau))
 // - tau is concave and decreasing, so from a start left of the root the first step lands right of
 // it by the curvature over the distance, and from the right the iterates decrease monotonically
 // by about a sigma / fact per step while Vf is far above its root value.  From 0 the first step
 // overshoots by about FltZ Vf (megapascals at seismic slip rates, several a sigma), from the
 // current stress by the step's stress change: fewer iterations, the same root to within the
-// stopping tolerance 0.001 a sigma.
+// stopping tolerance 0.001 a sigma.  (Evaluating the exponentials on the FP32 unit after an FP64
+// range reduction took the dz480 fault kernel from 30.5 to 24.4 us, but that kernel runs beside
+// the longer chain of the other rows, so the step did not get faster, and the slip rate's error
+// against FP64 after 60 dynamic steps rose from below 1e-6 to 1.1e-6: not kept.)
 __device__ __forceinline__ int dev_NR_warm(double fo, double Vo, double cca, double ccb, double Seff, double tau,
                                            double tauo, double psi, double FltZ, double FltVfree, double* Vf_out,
                                            double* tau_out) {

@@ -2,6 +2,7 @@
 #include "mg.h"
 #include "reduce.cuh"
 #include "epi.cuh"
+#include "mg_pt.cuh"
 #include <cmath>
 #include <random>
 #include <utility>
@@ -14,18 +15,8 @@ __global__ void k_stencil(const T* __restrict__ A, const T* __restrict__ x, T* _
                           OpEpi<T> E) {
     EQC_GRID_WAIT();
     const int64_t N = (int64_t)cx * cy;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        const int ix = (int)(i % cx), iy = (int)(i / cx);
-        T s = T(0);
-        if (iy >= 1) {
-#pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                const int gx = ix + (k % 3) - 1, gy = iy + (k / 3) - 1;
-                if (gx >= 0 && gx < cx && gy >= 1 && gy < cy) s += A[k * N + i] * x[(int64_t)gy * cx + gx];
-            }
-        }
-        epi_store1(E, y, i, s);
-    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+        epi_store1(E, y, i, stencil_pt<T>(A, x, cx, cy, N, i, LdPlain()));
 }
 
 // xf[fine] += sum_{a,b} wx_a wy_b xc[coarse]   (fine rows >= 1)
@@ -38,38 +29,9 @@ __global__ void k_prolong_add(const T* __restrict__ xc, T* __restrict__ xf, int 
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % nfx), iy = (int)(i / nfx);
         if (iy == 0) continue;
-        T s = T(0);
-#pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            const T wb = wy[2 * iy + b];
-            if (wb == T(0)) continue;
-            const int cyi = py[2 * iy + b];
-#pragma unroll
-            for (int a = 0; a < 2; ++a) {
-                const T wa = wx[2 * ix + a];
-                if (wa != T(0)) s += wa * wb * xc[(int64_t)cyi * ldc + px[2 * ix + a]];
-            }
-        }
-        xf[(int64_t)iy * ldf + ix] += s;
+        T* o = xf + (int64_t)iy * ldf + ix;
+        *o = add_rn<T>(*o, prolong_pt<T>(xc, ldc, px, py, wx, wy, ix, iy, LdPlain()));
     }
-}
-
-// The coarse level's first Chebyshev step from x = 0, fused into the restriction that produces
-// its right-hand side (k_cheb_first with with_x = 0): r = Dinv b ; d = r / theta ; x = d.
-template <class T>
-struct ChebFirst {
-    const T* dinv = nullptr;   // null: not fused
-    T *x = nullptr, *r = nullptr, *d = nullptr;
-    T inv_theta = T(0);
-};
-template <class T>
-__device__ __forceinline__ void cheb_first_pt(const ChebFirst<T>& F, int64_t i, T b) {
-    if (!F.dinv) return;
-    const T ri = mul_rn<T>(F.dinv[i], b);
-    const T di = mul_rn<T>(ri, F.inv_theta);
-    F.r[i] = ri;
-    F.d[i] = di;
-    F.x[i] = di;
 }
 
 // bc[coarse] = sum over restriction lists of rf[fine]  (coarse rows >= 1; row 0 = 0)
@@ -82,17 +44,7 @@ __global__ void k_restrict(const T* __restrict__ rf, T* __restrict__ bc, int ncx
     const int64_t N = (int64_t)ncx * ncy;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int cxi = (int)(i % ncx), cyi = (int)(i / ncx);
-        T s = T(0);
-        if (cyi >= 1) {
-            for (int q = rpy[cyi]; q < rpy[cyi + 1]; ++q) {
-                const int fy = riy[q];
-                if (fy == 0) continue;
-                const T wq = rwy[q];
-                T sx = T(0);
-                for (int p = rpx[cxi]; p < rpx[cxi + 1]; ++p) sx += rwx[p] * rf[(int64_t)fy * ldf + rix[p]];
-                s += wq * sx;
-            }
-        }
+        const T s = restrict_pt<T>(rf, ldf, rpx, rix, rwx, rpy, riy, rwy, cxi, cyi, LdPlain());
         bc[(int64_t)cyi * ldc + cxi] = s;
         cheb_first_pt(F, (int64_t)cyi * ldc + cxi, s);
     }
@@ -164,13 +116,8 @@ template <class T>
 __global__ void k_cheb_first(T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, const T* __restrict__ b,
                              const T* __restrict__ t, const T* __restrict__ Dinv, int64_t n, T inv_theta, int with_x) {
     EQC_GRID_WAIT();
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T ri = with_x ? mul_rn<T>(Dinv[i], sub_rn<T>(b[i], t[i])) : mul_rn<T>(Dinv[i], b[i]);
-        const T di = mul_rn<T>(ri, inv_theta);
-        r[i] = ri;
-        d[i] = di;
-        x[i] = with_x ? add_rn<T>(x[i], di) : di;
-    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        cheb_first_step_pt<T>(x, r, d, b, t, Dinv, i, inv_theta, with_x != 0, LdPlain());
 }
 // Chebyshev, later step: r -= Dinv t (t = A d) ; d = c1 d + c2 r ; x += d
 template <class T>
@@ -195,25 +142,11 @@ __global__ void k_sub(const T* __restrict__ b, const T* __restrict__ t, T* __res
 // x[cx + k] = sum_j Cinv[k][j] b[cx + j]  (one warp per row).  Accumulates in T: FP32 for the
 // FP32 cycle (a preconditioner; GB300's FP64 rate would make this the slowest kernel of it).
 template <class T>
-__device__ __forceinline__ T warp_sum_t(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-template <class T>
 __global__ void k_dense_mv(const T* __restrict__ Cinv, const T* __restrict__ b, T* __restrict__ x, int n, int off) {
     EQC_GRID_WAIT();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= n) return;
-    const T* row = Cinv + (int64_t)warp * n;
-    T s0 = T(0), s1 = T(0);
-    int j = lane;
-    for (; j + 32 < n; j += 64) {
-        s0 += row[j] * b[off + j];
-        s1 += row[j + 32] * b[off + j + 32];
-    }
-    if (j < n) s0 += row[j] * b[off + j];
-    const T s = warp_sum_t(s0 + s1);
+    const T s = dense_row<T>(Cinv, b, n, off, warp, lane, LdPlain());
     if (lane == 0) x[off + warp] = s;
 }
 template <class T>
@@ -318,31 +251,45 @@ static int64_t level_size(Handle& h, int l) {
 // first step (from x = 0) already ran inside the restriction that produced b.  Later steps run
 // fused into the operator (r, x updated in place, the direction alternating between the d and t
 // work vectors) when the level's operator kernel has the epilogue.
+// The Chebyshev smoother's coefficients on level l (0: the spectral-element level): 1/theta of
+// the first step and (c1[k], c2[k]) of steps k = 1..deg-1.
+static void cheb_coeffs(const MGHier& m, int l, int deg, double* inv_theta, double* c1, double* c2) {
+    const double lmax = (l == 0) ? m.lmax0 : m.lev[l - 1].lmax;
+    const double lmin = lmax / m.lo_ratio;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    const double sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    *inv_theta = 1.0 / theta;
+    for (int k = 1; k < deg; ++k) {
+        const double rho_new = 1.0 / (2.0 * sigma - rho);
+        c1[k] = rho_new * rho;
+        c2[k] = 2.0 * rho_new / delta;
+        rho = rho_new;
+    }
+}
+
 template <class T>
 static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x, bool first_done = false) {
     MGHier& m = *h.mg;
     MGWork& w = m.work[l];
     const int64_t n = level_size(h, l);
     const T* Dinv = (l == 0) ? Sel<T>::Di0(m) : Sel<T>::Di(m.lev[l - 1]);
-    const double lmax = (l == 0) ? m.lmax0 : m.lev[l - 1].lmax;
-    const double lmin = lmax / m.lo_ratio;
-    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
-    const double sigma = theta / delta;
-    double rho = 1.0 / sigma;
+    const int deg = (l == 0) ? m.deg : m.deg_coarse;
+    std::vector<double> cc1(std::max(deg, 1)), cc2(std::max(deg, 1));
+    double inv_theta = 0.0;
+    cheb_coeffs(m, l, deg, &inv_theta, cc1.data(), cc2.data());
     T* r = Sel<T>::r(w);
     T* d = Sel<T>::d(w);
     T* t = Sel<T>::t(w);
     if (!first_done) {
         if (with_x) level_apply<T>(h, l, x, t);
-        k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)(1.0 / theta), with_x ? 1 : 0);
+        k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)inv_theta, with_x ? 1 : 0);
         count_launch();
     }
-    const int deg = (l == 0) ? m.deg : m.deg_coarse;
     T* dcur = d;
     T* dnext = t;
     for (int k = 1; k < deg; ++k) {
-        const double rho_new = 1.0 / (2.0 * sigma - rho);
-        const T c1 = (T)(rho_new * rho), c2 = (T)(2.0 * rho_new / delta);
+        const T c1 = (T)cc1[k], c2 = (T)cc2[k];
         OpEpi<T> E;
         E.mode = 2;
         E.r = r;
@@ -359,16 +306,15 @@ static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x, bool firs
             k_cheb_step<T><<<vb(n), 256, 0, h.stream>>>(x, r, dcur, t, Dinv, n, c1, c2);
             count_launch();
         }
-        rho = rho_new;
     }
     EQC_CHECK_LAUNCH();
 }
 
 // 1 / theta of level l's Chebyshev interval (as chebyshev() computes it)
 static double cheb_inv_theta(const MGHier& m, int l) {
-    const double lmax = (l == 0) ? m.lmax0 : m.lev[l - 1].lmax;
-    const double lmin = lmax / m.lo_ratio;
-    return 1.0 / (0.5 * (lmax + lmin));
+    double it = 0.0;
+    cheb_coeffs(m, l, 1, &it, nullptr, nullptr);
+    return it;
 }
 
 // first_done: the restriction that produced b already took level l's first smoothing step.

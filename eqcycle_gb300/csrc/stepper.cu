@@ -396,12 +396,12 @@ static_assert(sizeof(CtlAcc) == 3 * sizeof(double), "the fault kernel's partials
 static_assert(FNT == 32, "the dynamic fault kernel reduces with one warp per CTA");
 constexpr double DTMAX = 50.0 * 24 * 60 * 60;   // src/dtevol.jl:7
 __device__ __forceinline__ CtlAcc ctl_init() { return CtlAcc{-INFINITY, 0x7fffffff, 0, DTMAX}; }
-__device__ __forceinline__ void ctl_add(CtlAcc& c, int k, double vk, const FaultArgs& f, double Vpl) {
+__device__ __forceinline__ void ctl_add(CtlAcc& c, int k, double vk, double xilf, int nfbc0, double Vpl) {
     if (vk > c.vmax) { c.vmax = vk; c.imax = k; }
     if (vk != vk) c.nan = 1;
-    if (k >= f.NFBC0) {
+    if (k >= nfbc0) {
         const double sr = fabs(2 * vk + Vpl);
-        if (sr * DTMAX > f.XiLf[k]) c.dmin = fmin(c.dmin, f.XiLf[k] / sr);
+        if (sr * DTMAX > xilf) c.dmin = fmin(c.dmin, xilf / sr);
     }
 }
 __device__ __forceinline__ void ctl_merge(CtlAcc& c, const CtlAcc& o) {
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
     __shared__ CtlAcc sh[32];
     const double Vpl = C->Vpl;
     CtlAcc c = ctl_init();
-    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) ctl_add(c, k, v[k], f, Vpl);
+    for (int k = threadIdx.x; k < f.Nf; k += blockDim.x) ctl_add(c, k, v[k], f.XiLf[k], f.NFBC0, Vpl);
     c = ctl_warp(c);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
     __syncthreads();
@@ -463,8 +463,8 @@ __global__ void __launch_bounds__(FT) k_control(const double* __restrict__ v, Fa
 // The fault row of the mixed method's dynamic step, from a = -(K d)[iFlt] (t0, the FP64 strip
 // apply of the predicted displacement, on the steps that refresh K d; else K d += q0) to the end
 // of the step, then the control of k_control: the creeping nodes' a = 0 and the absorbing term
-// of the fault's bottom node (main.jl:314-318), the friction Newton solves (warm-started,
-// dev_NR_warm) and a[iFlt] -= FltB tau (main.jl:321-331), a *= 1/M, v += dt/2 a,
+// of the fault's bottom node (main.jl:314-318), the friction Newton solves (dev_NR_warm:
+// warm-started) and a[iFlt] -= FltB tau (main.jl:321-331), a *= 1/M, v += dt/2 a,
 // creeping nodes a = v = 0 (main.jl:336-344); the last CTA to finish (counted in *count, which
 // it clears again) combines the per-CTA partials in part[], reduces Vfmax, switches the regime and
 // takes the next dt.  It runs beside the end of the step on the other rows, which it shares no
@@ -480,53 +480,65 @@ __global__ void __launch_bounds__(FNT) k_dyn_fault_nm(double* __restrict__ a, do
     const int full = C->kd_full;
     CtlAcc acc = ctl_init();
     for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < f.Nf; k += blockDim.x * gridDim.x) {
-        const double vk0 = v[k];
+        // every input is loaded before the first store: through FaultArgs' pointers (which may
+        // alias for all the compiler knows) a load after a store waits for it, and the node's
+        // work is one thread's latency chain
+        const double vk0 = v[k], vpre = f.vPre[k], Mf = __ldg(f.Mf + k), psi = f.psi[k], tau_c = f.tau[k];
+        const double tauo = __ldg(f.tauo + k), FltB = __ldg(f.FltB + k), iM = __ldg(invM + k);
+        const double xilf = __ldg(f.XiLf + k), tau2_old = f.tau2[k], psi2_old = f.psi2[k];
+        const int bc = __ldg(f.bcflag + k), cr = __ldg(f.creep + k);
+        const bool fr = k >= f.NFBC0;
+        double xLf = 0, Vo = 0, fo = 0, cca = 0, ccb = 0, Seff = 0, FltZ = 0;
+        if (fr) {
+            xLf = __ldg(f.xLf + k);
+            Vo = __ldg(f.Vo + k);
+            fo = __ldg(f.fo + k);
+            cca = __ldg(f.cca + k);
+            ccb = __ldg(f.ccb + k);
+            Seff = __ldg(f.Seff + k);
+            FltZ = __ldg(f.FltZ + k);
+        }
         // K d on the fault row as on the other rows: recomputed in FP64 (t0) on the steps that
         // refresh it (the full FP64 apply beside this kernel stores it), else K d += K dd (q0, the
         // FP32 apply of the increment on the fault's element row, whose row 0 has the bits of the
         // full FP32 apply's: every row's K d then carries the same FP32 rounding.  A strip kernel
         // with another summation order let the fault row's K d drift from its neighbours', a net
         // force that made the displacement error ten times larger after 300 steps.)
-        double kd;
-        if (full) {
-            kd = t0[k];
-        } else {
-            kd = __dadd_rn(Kd[k], f32_to_f64(q0[k]));
-            Kd[k] = kd;
-        }
+        const double kd = full ? t0[k] : __dadd_rn(Kd[k], f32_to_f64(q0[k]));
         double a0 = -kd;
-        if (f.bcflag[k]) a0 = 0.0;
+        if (bc) a0 = 0.0;
         if (k == 0 && hasL0) a0 = a0 - cL0 * vk0;
-        const double vfree = 2 * vk0 + 2 * hdt * a0 / f.Mf[k];
-        f.FltVfree[k] = vfree;
-        const double vf = 2 * f.vPre[k] + Vpl;
-        f.Vf[k] = vf;
-        if (k >= f.NFBC0) {
-            const double p1 = dev_IDS(f.xLf[k], f.Vo[k], f.psi[k], dt, vf, 1e-5);
-            f.psi1[k] = p1;
-            double V1, T1;
+        const double vfree = 2 * vk0 + 2 * hdt * a0 / Mf;
+        const double vf = 2 * vpre + Vpl;
+        double p1 = 0, V1 = 0, T1 = 0, p2 = psi2_old, V2 = 0, T2 = tau2_old;
+        if (fr) {
+            p1 = dev_IDS(xLf, Vo, psi, dt, vf, 1e-5);
             // the first search starts from the node's current shear stress (tau + tauo)
-            dev_NR_warm(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], f.tau[k] + f.tauo[k], f.tauo[k], p1, f.FltZ[k],
-                        vfree, &V1, &T1);
+            dev_NR_warm(fo, Vo, cca, ccb, Seff, tau_c + tauo, tauo, p1, FltZ, vfree, &V1, &T1);
+            if (vf > 1e10 || isnan(vf) || isnan(T1)) atomicMin(&C->fail, k + 1);
+            p2 = dev_IDS2(xLf, Vo, psi, p1, dt, vf, V1);
+            dev_NR_warm(fo, Vo, cca, ccb, Seff, T1, tauo, p2, FltZ, vfree, &V2, &T2);
+        }
+        double t = T2 - tauo;
+        if (cr) t = 0.;
+        double am = __dmul_rn(a0 - FltB * t, iM), vk = __fma_rn(hdt, am, vk0);
+        if (cr) am = vk = 0.0;
+        if (!full) Kd[k] = kd;
+        f.FltVfree[k] = vfree;
+        f.Vf[k] = vf;
+        if (fr) {
+            f.psi1[k] = p1;
             f.Vf1[k] = V1;
             f.tau1[k] = T1;
-            if (vf > 1e10 || isnan(vf) || isnan(T1)) atomicMin(&C->fail, k + 1);
-            const double p2 = dev_IDS2(f.xLf[k], f.Vo[k], f.psi[k], p1, dt, vf, V1);
             f.psi2[k] = p2;
-            double V2, T2;
-            dev_NR_warm(f.fo[k], f.Vo[k], f.cca[k], f.ccb[k], f.Seff[k], T1, f.tauo[k], p2, f.FltZ[k], vfree, &V2, &T2);
             f.Vf2[k] = V2;
             f.tau2[k] = T2;
         }
-        double t = f.tau2[k] - f.tauo[k];
-        if (f.creep[k]) t = 0.;
         f.tau[k] = t;
-        f.psi[k] = f.psi2[k];
-        double am = __dmul_rn(a0 - f.FltB[k] * t, invM[k]), vk = __fma_rn(hdt, am, vk0);
-        if (f.creep[k]) am = vk = 0.0;
+        f.psi[k] = p2;
         a[k] = am;
         v[k] = vk;
-        ctl_add(acc, k, vk, f, Vpl);
+        ctl_add(acc, k, vk, xilf, f.NFBC0, Vpl);
     }
     acc = ctl_warp(acc);
     if (threadIdx.x == 0) {
