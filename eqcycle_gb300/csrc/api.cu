@@ -233,6 +233,10 @@ static void create(Handle& h, const eqc_model& m, const eqc_material* mat) {
                              &h.q64, &h.Kd})
         b->alloc(N);
     for (DBuf<float>* b : {&h.r32, &h.z32, &h.p32, &h.q32, &h.x32, &h.g32}) b->alloc(N);
+    if (h.opt.precision == EQC_MIXED && std::getenv("EQC_NO_DF_UPDATE") == nullptr) {
+        h.dx64.alloc(N);    // the intermediate reliable updates' correction and its K dx
+        h.kdx64.alloc(N);
+    }
     if (!mat) {
         std::vector<double> Mlay(N, 1.0);
         for (int64_t g = 0; g < m.nglob; ++g) Mlay[h.ref2lay[g]] = m.M[g];

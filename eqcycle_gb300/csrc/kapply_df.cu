@@ -1,9 +1,10 @@
 // K1 in double-float: y = sign * K x for FP64 x and y, evaluated with FP32 operations on
 // unevaluated hi + lo pairs (df.cuh), ~1e-14 relative per operation, for callers that need an
-// FP64-class apply at the FP32 rate (eqc_apply_K_device dtype 2).  The mixed solver's true
-// residuals b - K_II x do not use it: early in a cycle |K||x| / |b| is ~1e2 and double-float
-// would do, but late in a cycle the displacement grows until the 1e-14 error floors the residual
-// near 1e-5 of |b|, above the CG tolerance (measured), so those stay FP64.
+// FP64-class apply at the FP32 rate (eqc_apply_K_device dtype 2, and the mixed solver's
+// intermediate reliable updates, r -= K dx with dx the correction since the previous update).
+// The solver's full true residuals b - K_II x do not use it: late in a cycle the displacement
+// grows until the 1e-14 error of K x floors the residual near 1e-5 of |b|, above the CG
+// tolerance (measured), so those stay FP64; K dx has the size of the residual it corrects.
 //
 // Layout as k_apply_rows: one lane per element, one warp per element row of 31 elements plus a
 // halo lane, ROWS element rows per CTA plus a halo warp; the line contractions in even-odd form.
@@ -40,8 +41,10 @@ __device__ __forceinline__ df shfl_up_df(df v) {
 template <int ROWS>
 __global__ void __launch_bounds__(32 * (ROWS + 1), 2)
     k_apply_df(const double* __restrict__ x, double* __restrict__ y, const float* __restrict__ Whi,
-               const float* __restrict__ Wlo, Layout L, df c1, df c2, double sign, int zero_row0) {
+               const float* __restrict__ Wlo, Layout L, df c1, df c2, double sign, int zero_row0,
+               const int* gate, int gate_val) {
     EQC_GRID_WAIT();
+    if (gate && *gate != gate_val) return;
     __shared__ float Th[ROWS + 1][5][32], Tl[ROWS + 1][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int ex = (int)blockIdx.x * 31 - 1 + lane;
@@ -157,13 +160,14 @@ void set_H_df(const double* H, cudaStream_t s) {
     EQC_CUDA(cudaStreamSynchronize(s));
 }
 
-bool apply_K_df(Handle& h, const double* x, double* y, double sign, int mode, cudaStream_t s) {
+bool apply_K_df(Handle& h, const double* x, double* y, double sign, int mode, cudaStream_t s, const int* gate,
+                int gate_val) {
     if (!h.df_ok || mode > 1 || !h.W32lo.p || (reinterpret_cast<uintptr_t>(y) & 15)) return false;
     constexpr int R = 6;
     const Layout& L = h.L;
     dim3 g((L.NelX + 1 + 30) / 31, (L.NelY + 1 + R - 1) / R);
     k_apply_df<R><<<g, 32 * (R + 1), 0, s>>>(x, y, h.W32p.p, h.W32lo.p, L, host_df(h.c1), host_df(h.c2), sign,
-                                             mode == 1 ? 1 : 0);
+                                             mode == 1 ? 1 : 0, gate, gate_val);
     EQC_CHECK_LAUNCH();
     count_launch();
     return true;

@@ -59,6 +59,9 @@ struct CGState {
     int it, maxit;
     int done;          // 0 running, 1 converged, 2 maxit reached, 3 non-finite residual
     int need_update;   // mixed precision: a reliable update is due
+    int upd_incr;      // ... and it is an intermediate one (the residual fell by the update factor,
+                       // the loop goes on): r -= K dx in double-float; else b - K x in FP64
+    int incr_ok;       // this solve's updates may take the double-float form
     int restart;       // the next direction update starts afresh (beta = 0)
     double sigma;      // mixed precision: the FP32 recurrence vectors hold sigma * (true value),
                        // sigma a power of two near 1 / ||b|| (keeps tiny residuals out of
@@ -148,6 +151,7 @@ struct Handle {
     double H[25];
     // node arrays [L.size()]
     DBuf<double> M, d, v, a, dPre, tmp64a, tmp64b, tmp64c;
+    DBuf<double> dx64, kdx64;   // mixed CG: correction since the last reliable update, -K_II of it
     DBuf<double> Kd;          // K d of the mixed-precision dynamic step
     DBuf<double> invM;        // 1 / M (mixed-precision dynamic step)
     DBuf<double> diag64;   // diagonal of K (rows >= 1), Jacobi preconditioner
@@ -208,7 +212,8 @@ inline ApplyArgs<float> args32(Handle& h) {
 void tma_init(Handle& h);
 void set_H_df(const double* H, cudaStream_t s);
 // y = sign K x (FP64 vectors, mode 0/1) in double-float arithmetic; false when unavailable.
-bool apply_K_df(Handle& h, const double* x, double* y, double sign, int mode, cudaStream_t s);
+bool apply_K_df(Handle& h, const double* x, double* y, double sign, int mode, cudaStream_t s,
+                const int* gate = nullptr, int gate_val = 0);
 void tma_init_for(TmaCache& c, const Layout& L, const float* W32p, const double* W64p);
 // FP32 apply y = K x (mode 0/1 as apply_K) whose owned nodes are finished by the epilogue E
 // (residual or Chebyshev step) instead of stored; false when the selected kernel has none.

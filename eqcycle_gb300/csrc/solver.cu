@@ -106,34 +106,68 @@ __global__ void k_jacobi(const T* __restrict__ r, const T* __restrict__ dg, T* _
         z[i] = r[i] / dg[i];
 }
 
-// x64 += (double) y32 / sigma ; y32 = 0   (sigma a power of two: the division is exact)
-__global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, float* __restrict__ y, int64_t n,
-                                                      const CGState* S) {
+// x64 += (double) y32 / sigma ; y32 = 0   (sigma a power of two: the division is exact); for an
+// intermediate reliable update (S->upd_incr) also dx64 += y32: dx64 is sigma times x's change since
+// r64 was last exact, whose K dx updates the residual (in the recurrence's scaled units, so that
+// the steady-sliding start's 1e-25 m increments stay inside double-float's range).
+__global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, float* __restrict__ y,
+                                                      double* __restrict__ dx, int64_t n, const CGState* S) {
     EQC_GRID_WAIT();
     const double inv = 1.0 / S->sigma;
+    const bool incr = dx && S->upd_incr;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
-        double xx[4];
+        double xx[4], dd[4];
         float yy[4];
         ld4(x + i, xx);
         ld4(y + i, yy);
+        if (incr) ld4(dx + i, dd);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) xx[k] += (double)yy[k] * inv;
+        for (int k = 0; k < 4; ++k) {
+            xx[k] += (double)yy[k] * inv;
+            if (incr) dd[k] += (double)yy[k];
+        }
         st4(x + i, xx);
+        if (incr) st4(dx + i, dd);
         const float zero[4] = {0.f, 0.f, 0.f, 0.f};
         st4(y + i, zero);
     }
 }
-// r32 = (float) (sigma r64) ; S->rr = sigma^2 r64.r64
-__global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(const double* __restrict__ r64, float* __restrict__ r32,
-                                                             int64_t n, double* part, unsigned* count, CGState* S) {
+
+// dx64 = sigma times the kept initial-guess increment (r64 is the residual without it), else 0.
+__global__ void k_dx_init(double* __restrict__ dx, const float* __restrict__ g, const CGState* S, int64_t n) {
+    EQC_GRID_WAIT();
+    const bool keep = g && S->guess_keep;
+    const double sg = S->sigma;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dx[i] = keep ? (double)g[i] * sg : 0.0;
+}
+// [intermediate reliable update (kdx given and S->upd_incr): r64 += kdx / sigma, kdx the
+// double-float -K dx of the scaled change] ; r32 = (float) (sigma r64) ; S->rr = sigma^2 r64.r64
+// (kdx given: a reliable update's end; r64 is then exact for x, so dx64 = 0.)
+__global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(double* __restrict__ r64, float* __restrict__ r32,
+                                                             int64_t n, double* part, unsigned* count, CGState* S,
+                                                             const double* __restrict__ kdx, double* __restrict__ dx) {
     EQC_GRID_WAIT();
     __shared__ double sh[32];
     const double sg = S->sigma;
+    const bool incr = kdx && S->upd_incr;
     double s = 0.0;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double v[4];
         float f[4];
         ld4(r64 + i, v);
+        if (incr) {
+            const double inv = 1.0 / sg;   // a power of two: exact
+            double t[4];
+            ld4(kdx + i, t);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] = __fma_rn(t[k], inv, v[k]);
+            st4(r64 + i, v);
+        }
+        if (dx) {
+            const double zero[4] = {0.0, 0.0, 0.0, 0.0};
+            st4(dx + i, zero);
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             f[k] = (float)(v[k] * sg);
@@ -160,8 +194,11 @@ static inline dim3 vgrid() { return dim3(VEC_BLOCKS); }
 // cudaGraphSetConditional for its node (concurrent calls on one handle are undefined).
 
 // Start of a solve: S->bb, S->rr hold ||b||^2 and ||r0||^2.
-__global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, cudaGraphConditionalHandle hw, int use_cond) {
+__global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, int incr_ok, cudaGraphConditionalHandle hw,
+                          int use_cond) {
     EQC_GRID_WAIT();
+    S->incr_ok = incr_ok;
+    S->upd_incr = 0;
     const double nb = sqrt(S->bb), r = sqrt(S->rr) / S->sigma;
     const double reltol = (rule == EQC_TOL_R0 ? r : nb) * tol;
     S->nb = nb;
@@ -206,6 +243,8 @@ __global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandl
     }
     S->res = rs;
     S->need_update = need;
+    // a certifying update (the loop would stop) recomputes b - K x in FP64
+    S->upd_incr = (need && rs > S->reltol && S->it < S->maxit && S->incr_ok) ? 1 : 0;
     if (use_cond) cudaGraphSetConditional(hi, need ? 1u : 0u);
 }
 
@@ -369,7 +408,7 @@ static void setup_residual_full(Handle& h, bool mixed) {
     apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);     // r = -(K d)_I
     if (mixed) {
         k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p,
-                                                             h.red_count.p, S);
+                                                             h.red_count.p, S, nullptr, h.dx64.p ? h.dx64.p + ld : nullptr);
         EQC_CHECK_LAUNCH();
         count_launch();
     } else {
@@ -385,7 +424,7 @@ static void setup_residual_carry(Handle& h, const float* guess) {
     apply_K<double>(h.tmp64b.p, h.tmp64c.p, args64(h), -1.0, 2, h.stream);
     k_carry_rows<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.tmp64c.p + ld, 4 * ld);
     k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p,
-                                                         h.red_count.p, h.cg.p);
+                                                         h.red_count.p, h.cg.p, nullptr, h.dx64.p ? h.dx64.p + ld : nullptr);
     EQC_CHECK_LAUNCH();
     count_launch(2);
     if (guess) {
@@ -397,6 +436,11 @@ static void setup_residual_carry(Handle& h, const float* guess) {
                                                               h.r64.p + ld, n);
         EQC_CHECK_LAUNCH();
         count_launch(3);
+        if (h.dx64.p) {   // r64 is the residual without the kept increment
+            k_dx_init<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.dx64.p + ld, guess + ld, h.cg.p, n);
+            EQC_CHECK_LAUNCH();
+            count_launch();
+        }
     }
 }
 
@@ -445,16 +489,31 @@ static void iter_mixed_a(Handle& h, double delta, cudaGraphConditionalHandle hi,
 }
 
 // Reliable update: x += y ; r = b - K_II x in FP64 ; r32 = r ; S->rr = ||r||^2.
+// An intermediate update (the recurrence residual fell by the update factor and the loop goes on)
+// instead computes r -= K_II dx with the double-float apply of the correction dx folded since the
+// previous update (69 against 160 us on dz480): K dx has the size of the residual it corrects, so
+// the double-float error stays far below the residual left.  The update that certifies
+// convergence recomputes b - K_II x with the FP64 apply: the full K x's double-float error would
+// floor the residual near 1e-5 of |b| late in a cycle (|K||x| / |b| large; measured).  Both
+// forms run as gated launches (ApplyArgs::gate on S->upd_incr).
+static int incr_updates(const Handle& h, bool mixed) {
+    return (mixed && h.df_ok && h.dx64.p && h.kdx64.p) ? 1 : 0;
+}
 static void update_mixed(Handle& h) {
     const Layout& L = h.L;
     const int64_t ld = L.ld, n = L.size() - ld;
     CGState* S = h.cg.p;
-    k_fold<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.d.p + ld, h.x32.p + ld, n, S);
-    // FP64, not the double-float apply: late in a cycle |K||x| / |b| grows until its ~1e-14
-    // relative error floors the true residual near 1e-5 of |b| (measured), above the tolerance
-    apply_K<double>(h.d.p, h.r64.p, args64(h), -1.0, 1, h.stream);
+    const bool incr = incr_updates(h, true) != 0;
+    k_fold<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.d.p + ld, h.x32.p + ld, incr ? h.dx64.p + ld : nullptr, n, S);
+    ApplyArgs<double> a64 = args64(h);
+    if (incr) {
+        a64.gate = &S->upd_incr;
+        a64.gate_val = 0;
+        apply_K_df(h, h.dx64.p, h.kdx64.p, -1.0, 1, h.stream, &S->upd_incr, 1);   // -K_II dx
+    }
+    apply_K<double>(h.d.p, h.r64.p, a64, -1.0, 1, h.stream);                    // r = -(K d)_I
     k_demote_norm<<<vgrid(), VEC_THREADS, 0, h.stream>>>(h.r64.p + ld, h.r32.p + ld, n, h.red_part.p, h.red_count.p,
-                                                         S);
+                                                         S, incr ? h.kdx64.p + ld : nullptr, incr ? h.dx64.p + ld : nullptr);
     EQC_CHECK_LAUNCH();
     count_launch(2);
 }
@@ -513,7 +572,7 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry, con
     if (graph) {
         // k_cg_init (upstream of the while node) sets the node's first value
         const cudaGraphConditionalHandle hw = cond_handle(h);
-        k_cg_init<<<1, 1, 0, h.stream>>>(S, tol, maxit, h.opt.tol_rule, hw, 1);
+        k_cg_init<<<1, 1, 0, h.stream>>>(S, tol, maxit, h.opt.tol_rule, incr_updates(h, mixed), hw, 1);
         count_launch();
         const int64_t t0 = capture_tally();
         cond_begin(h, cudaGraphCondTypeWhile, hw);
@@ -541,7 +600,7 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry, con
         }
         cond_end(h);
     } else {
-        k_cg_init<<<1, 1, 0, h.stream>>>(S, tol, maxit, h.opt.tol_rule, 0, 0);
+        k_cg_init<<<1, 1, 0, h.stream>>>(S, tol, maxit, h.opt.tol_rule, incr_updates(h, mixed), 0, 0);
         count_launch();
         const CGState* hs = &read_cg(h);
         while (hs->done == 0) {

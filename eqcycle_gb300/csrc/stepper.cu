@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(FNT) k_qs_begin(double* __restrict__ d, const 
 // last step was quasi-static, the extrapolated initial guess d += g with
 // g = (dt / dt_prev) (d - dPre_old) (g also kept in FP32 for the residual correction).
 __global__ void k_qs_begin_bulk(double* __restrict__ d, double* __restrict__ dPre, float* __restrict__ g, int64_t n,
-                                int64_t ld, int extrap, const Ctrl* C) {
+                                int64_t ld, int extrap, const Ctrl* C, int round_g) {
     EQC_GRID_WAIT();
     const bool use = extrap && C->qs_prev && C->dt_prev > 0;
     const double ratio = use ? C->dt / C->dt_prev : 0.0;
@@ -51,8 +51,11 @@ __global__ void k_qs_begin_bulk(double* __restrict__ d, double* __restrict__ dPr
         dPre[i] = dn;
         if (i >= ld) {
             const double gi = use ? ratio * (dn - dp) : 0.0;
-            d[i] = dn + gi;
-            g[i] = (float)gi;
+            const float gf = (float)gi;
+            // round_g (mixed precision): the increment added is the FP32 one the solver accounts
+            // for (its intermediate reliable updates correct the residual by K of x's change)
+            d[i] = dn + (round_g ? (double)gf : gi);
+            g[i] = gf;
         } else {
             g[i] = 0.f;
         }
@@ -819,7 +822,8 @@ static void enqueue_qs(Handle& h, bool graph) {
     FaultArgs f = fargs(h, h.bcflag.p);
     const bool extrap = h.opt.guess == EQC_GUESS_EXTRAPOLATE;
     if (extrap) {
-        k_qs_begin_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.g32.p, n, L.ld, 1, h.ctrl.p);
+        k_qs_begin_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.g32.p, n, L.ld, 1, h.ctrl.p,
+                                                   h.opt.precision == EQC_MIXED ? 1 : 0);
         count_launch();
     } else {
         EQC_CUDA(cudaMemcpyAsync(h.dPre.p, h.d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));

@@ -146,3 +146,30 @@ def test_mixed_newmark_step_variants(eqclib, monkeypatch, variant):
     for k, (fused, seven) in errs.items():
         assert seven <= 1e-3, (k, seven)
         assert fused <= 1.5 * seven + 1e-7, (k, fused, seven)
+
+
+@pytest.mark.parametrize("name", ["homog48", "dz480"])
+def test_double_float_intermediate_updates(eqclib, monkeypatch, name):
+    """The mixed CG's intermediate reliable updates as r -= K dx with the double-float apply of the
+    correction since the previous update, against every update recomputing b - K x in FP64
+    (EQC_NO_DF_UPDATE): through quasi-static steps the CG iteration count stays within one per
+    solve and the displacement and state agree to the solver tolerance's scale (1e-6 relative),
+    every solve still certified on an FP64 residual (the run reports no CG failure)."""
+    from eqcycle_gb300 import EQC_GUESS_EXTRAPOLATE, EQC_MIXED, EQC_PC_AMG
+    cfg = preset(name)
+    P = set_parameters(cfg)
+    steps = 12 if name == "dz480" else 40
+    out = []
+    for env in (None, "EQC_NO_DF_UPDATE"):
+        monkeypatch.delenv("EQC_NO_DF_UPDATE", raising=False)
+        if env:
+            monkeypatch.setenv(env, "1")
+        with Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG, guess=EQC_GUESS_EXTRAPOLATE, cg_tol=1e-8) as s:
+            s.init(cfg.V_init)
+            st = s.run(steps)
+            assert st["qs_steps"] == steps
+            out.append((st["cg_iters"], st["qs_solves"], {k: s.state(k) for k in ("d", "psi", "tau")}))
+    (it_df, solves, a), (it_64, _, b) = out
+    assert abs(it_df - it_64) <= solves, (it_df, it_64)
+    for k in a:
+        assert np.max(np.abs(a[k] - b[k])) <= 1e-6 * np.max(np.abs(b[k])), k
