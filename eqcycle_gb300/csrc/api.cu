@@ -624,6 +624,7 @@ eqc_status eqc_get_state(eqc_handle* H, const char* name, double* out) {
         bool fault;
         DBuf<double>* b = state_buf(h, name, fault);
         if (!b) throw Error(EQC_E_ARG, std::string("unknown state ") + name);
+        if (b == &h.v || b == &h.a) materialize_dyn_state(h);
         if (fault) {
             b->download(out, h.F.Nf, h.stream);
             EQC_CUDA(cudaStreamSynchronize(h.stream));
@@ -643,6 +644,7 @@ eqc_status eqc_set_state(eqc_handle* H, const char* name, const double* in) {
         bool fault;
         DBuf<double>* b = state_buf(h, name, fault);
         if (!b) throw Error(EQC_E_ARG, std::string("unknown state ") + name);
+        if (b == &h.v || b == &h.a) materialize_dyn_state(h);   // the other one stays valid
         if (fault) {
             b->upload(in, h.F.Nf, h.stream);
         } else {

@@ -16,8 +16,12 @@ namespace eqc {
 // The end of a mixed-precision Newmark step at one node off the fault row (main.jl:309-339),
 // given t = (K dd)_i, the FP32 apply of the step's displacement increment: K d += t (FP64),
 // a = -K d, the absorbing terms a -= C v of the nodes on the edge x = -LX (column ix = 0, list
-// iBcL) and on the edge y = LY (row iy = ny - 1, list iBcT) in that order, then a /= M (a
-// multiply by 1/M) and v += dt/2 a.  The fault row is ended by the dynamic step's fault kernel.
+// iBcL) and on the edge y = LY (row iy = ny - 1, list iBcT) in that order (v the half-step
+// velocity), then a /= M (a multiply by 1/M).  The reference's v += dt/2 a and the next step's
+// predictor v += dt/2 a are taken as one update v += dt a, stored in v: the next step starts from
+// it (an FP64 operation and 24 bytes per node fewer), and nm_state_at recovers the step's end
+// velocity and acceleration where an output needs them.  The fault row is ended by the dynamic
+// step's fault kernel and keeps v and a.
 struct NmEpi {
     double *Kd = nullptr, *v = nullptr, *a = nullptr;
     const double* invM = nullptr;
@@ -25,6 +29,7 @@ struct NmEpi {
     const int *hasL = nullptr, *hasT = nullptr;    // ... and whether the node is in the list
     const double* hdt = nullptr;                    // dt / 2 (in the control block)
     const int* kd_full = nullptr;                   // nonzero: K d recomputed in FP64 this step
+    int* v_half = nullptr;                          // set: v holds the next half-step velocity
     int ld = 0, nx = 0, ny = 0;
 };
 
@@ -102,8 +107,23 @@ __device__ __forceinline__ void newmark_node(const NmEpi& N, int64_t i, int ix, 
     if (ix == 0 && N.hasL[iy]) ai = __dsub_rn(ai, __dmul_rn(N.cL[iy], vi));
     if (iy == N.ny - 1 && N.hasT[ix]) ai = __dsub_rn(ai, __dmul_rn(N.cT[ix], vi));
     ai = __dmul_rn(ai, N.invM[i]);
-    N.a[i] = ai;
-    N.v[i] = __fma_rn(hdt, ai, vi);
+    N.v[i] = __fma_rn(2.0 * hdt, ai, vi);
+}
+
+// The step's end velocity and acceleration at node i off the fault row while v holds the next
+// half-step velocity V = vh + dt a (newmark_node): a = (-K d - c vh) / M with c the node's
+// absorbing coefficients, so a = (-K d - c V) / M / (1 - c dt / M), exactly the stored formula
+// where c = 0; then v = V - dt/2 a.
+__device__ __forceinline__ void nm_state_at(const NmEpi& N, int64_t i, double hdt, double* v_end, double* a_end) {
+    const int iy = (int)(i / N.ld), ix = (int)(i - (int64_t)iy * N.ld);
+    const double V = N.v[i], im = N.invM[i];
+    double c = 0.0;
+    if (ix == 0 && N.hasL[iy]) c += N.cL[iy];
+    if (iy == N.ny - 1 && N.hasT[ix]) c += N.cT[ix];
+    double a = __dmul_rn(-N.Kd[i], im);
+    if (c != 0.0) a = ((-N.Kd[i] - c * V) * im) / (1.0 - c * 2.0 * hdt * im);
+    *a_end = a;
+    *v_end = __fma_rn(-hdt, a, V);
 }
 
 // Four consecutive nodes ix0 .. ix0 + 3 of row iy >= 1 (offset off, 32-byte aligned): 4-wide
@@ -116,18 +136,17 @@ __device__ __forceinline__ void newmark4(const NmEpi& N, int64_t off, int ix0, i
             if (ix0 + q < N.nx) newmark_node(N, off + q, ix0 + q, iy, t[q], add, hdt);
         return;
     }
-    double kd[4], vv[4], im[4], aa[4];
+    double kd[4], vv[4], im[4];
     ld4(N.Kd + off, kd);
     ld4(N.v + off, vv);
     ld4(N.invM + off, im);
+    const double dt = 2.0 * hdt;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         if (add) kd[q] = __dadd_rn(kd[q], f32_to_f64(t[q]));
-        aa[q] = __dmul_rn(-kd[q], im[q]);
-        vv[q] = __fma_rn(hdt, aa[q], vv[q]);
+        vv[q] = __fma_rn(dt, __dmul_rn(-kd[q], im[q]), vv[q]);
     }
     if (add) st4(N.Kd + off, kd);
-    st4(N.a + off, aa);
     st4(N.v + off, vv);
 }
 

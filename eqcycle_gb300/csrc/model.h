@@ -48,6 +48,8 @@ struct Ctrl {
     // mixed-precision Newmark: Kd = K d kept in FP64, updated by the FP32 apply of each step's
     // increment and refreshed in FP64 at the start of a dynamic phase and every KD_REFRESH steps
     int kd_valid, kd_age, kd_full;
+    int v_half;            // mixed method's dynamic phase: v off the fault row holds the next step's
+                           // half-step velocity v + dt/2 a (a there is not kept); 0: v and a as is
     double dt_step;        // dt of the dynamic step in progress (the mixed method's split predictor)
 };
 constexpr int KD_REFRESH = 256;
@@ -196,6 +198,10 @@ struct Handle {
     std::vector<double> delfref;
     ~Handle();
 };
+
+// stepper.cu: v and a off the fault row as the reference keeps them, where the mixed method's
+// dynamic phase holds the next half-step velocity in v (before a caller reads or sets them)
+void materialize_dyn_state(Handle& h);
 
 // kapply.cu
 void set_H(const double* H, cudaStream_t s);

@@ -116,7 +116,10 @@ __global__ void k_qs_end_bulk(const double* __restrict__ d, const double* __rest
                               double* __restrict__ a, int64_t ld, int64_t n, Ctrl* C) {
     EQC_GRID_WAIT();
     const double dt = C->dt;
-    if (blockIdx.x == 0 && threadIdx.x == 0) C->kd_valid = 0;   // d changed: no incremental K d
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        C->kd_valid = 0;   // d changed: no incremental K d
+        C->v_half = 0;     // v and a as the reference keeps them
+    }
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         if (i >= ld) v[i] = (d[i] - dPre[i]) / dt;
         a[i] = 0.;
@@ -200,7 +203,8 @@ __global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d,
 // folded in: vPre on the fault, v += dt/2 a, then d += dt v with that v (dt v + dt^2/2 a as one
 // product), and the FP32 increment dd32 = dt v for the FP32 apply.  Two FP64 operations per
 // node (GB300's FP64 rate bounds these vector kernels); the conversion to FP32 uses integer
-// operations.  The step runs as two launches over [i0, n): the node rows of the first element
+// operations.  Off the fault row in a dynamic phase (C->v_half) v already holds the half-step
+// velocity that the previous step's end stored: one FP64 operation, no read of a, no write of v.  The step runs as two launches over [i0, n): the node rows of the first element
 // row (lead = 1: the step's bookkeeping -- it, t, the choice how the step gets K d -- after which
 // the fault row's work can start), then the rest (lead = 0: the step's dt is read from dt_step,
 // since the control at the end of the fault row's work may already have replaced dt with the
@@ -208,10 +212,12 @@ __global__ void __launch_bounds__(256) k_dyn_predict_inc(double* __restrict__ d,
 __global__ void __launch_bounds__(256) k_dyn_predict_nm(double* __restrict__ d, double* __restrict__ v,
                                                         const double* __restrict__ a, double* __restrict__ vPre_f,
                                                         float* __restrict__ dd32, int Nf, int64_t i0, int64_t n,
-                                                        Ctrl* C, int lead) {
+                                                        int64_t n0_row, Ctrl* C, int lead) {
     EQC_GRID_WAIT();
     const double dt = lead ? C->dt : C->dt_step, hdt = C->half_dt;
     const float dt_hi = __double2float_rn(dt), dt_lo = __double2float_rn(dt - (double)dt_hi);
+    const int vm = C->v_half;
+    const int64_t ld = n0_row;
     if (lead && blockIdx.x == 0 && threadIdx.x == 0) {
         C->dt_step = dt;
         C->it += 1;
@@ -227,30 +233,33 @@ __global__ void __launch_bounds__(256) k_dyn_predict_nm(double* __restrict__ d, 
          i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double dd4[4], vv[4], aa[4];
         float f[4];
+        const bool full = !vm || i < ld;   // 4-entry groups never straddle rows (ld % 8 == 0)
         ld4(d + i, dd4);
         ld4(v + i, vv);
-        ld4(a + i, aa);
+        if (full) ld4(a + i, aa);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (i + k < Nf) vPre_f[i + k] = vv[k];
-            const double vh = __fma_rn(hdt, aa[k], vv[k]);
+            const double vh = full ? __fma_rn(hdt, aa[k], vv[k]) : vv[k];
             dd4[k] = __fma_rn(dt, vh, dd4[k]);
             f[k] = nm_incr32(vh, dt_hi, dt_lo);
             vv[k] = vh;
         }
         st4(d + i, dd4);
-        st4(v + i, vv);
+        if (full) st4(v + i, vv);
         st4(dd32 + i, f);
     }
 }
 
 // The end of the mixed Newmark step (NmEpi) on every real node off the fault row: K d += K dd
 // (t32, the FP32 apply of the step's increment, unless K d was just recomputed in FP64),
-// a = -K d with the absorbing terms, a *= 1/M, v += dt/2 a.
+// a = -K d with the absorbing terms, a *= 1/M, then the next step's half-step velocity
+// v + dt/2 a + dt/2 a into v (v_half: a is not stored; nm_state_at gives v and a on request).
 __global__ void __launch_bounds__(256) k_dyn_finish(NmEpi N, const float* __restrict__ t32) {
     EQC_GRID_WAIT();
     const double hdt = *N.hdt;
     if (*N.kd_full) t32 = nullptr;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *N.v_half = 1;   // read by the next step's predictors
     const int gx = N.ld / 4;
     const int64_t ng = (int64_t)gx * N.ny;   // groups of 4 nodes; row 0 is the fault kernel's
     for (int64_t g = gx + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
@@ -568,15 +577,36 @@ __global__ void __launch_bounds__(FNT) k_dyn_fault_nm(double* __restrict__ a, do
     }
 }
 
-// Gather d, v, a at receivers (main.jl:433-435) into out[3*ns].
+// Gather d, v, a at receivers (main.jl:433-435) into out[3*ns] (v and a of the step's end where
+// v holds the next half-step velocity).
 __global__ void k_gather_seis(const int64_t* idx, int ns, const double* d, const double* v, const double* a,
-                              double* out) {
+                              double* out, const Ctrl* C, NmEpi N) {
     EQC_GRID_WAIT();
     const int k = threadIdx.x;
     if (k < ns) {
-        out[k] = d[idx[k]];
-        out[ns + k] = v[idx[k]];
-        out[2 * ns + k] = a[idx[k]];
+        const int64_t g = idx[k];
+        double vg = v[g], ag = a[g];
+        if (C->v_half && g >= N.ld) nm_state_at(N, g, C->half_dt, &vg, &ag);
+        out[k] = d[g];
+        out[ns + k] = vg;
+        out[2 * ns + k] = ag;
+    }
+}
+
+// v and a of the step's end off the fault row, in place, where v holds the next half-step
+// velocity (before a caller reads or sets them); the host then clears v_half, after the launch,
+// so that every CTA reads the same flag.
+__global__ void k_nm_materialize(Ctrl* C, NmEpi N) {
+    EQC_GRID_WAIT();
+    if (!C->v_half) return;
+    const double hdt = C->half_dt;
+    const int64_t n = (int64_t)N.ld * N.ny;
+    for (int64_t i = N.ld + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i % N.ld >= N.nx) continue;
+        double ve, ae;
+        nm_state_at(N, i, hdt, &ve, &ae);
+        N.v[i] = ve;
+        N.a[i] = ae;
     }
 }
 
@@ -868,6 +898,7 @@ static NmEpi nm_args(Handle& h) {
     N.hasT = h.edgeThas.p;
     N.hdt = &h.ctrl.p->half_dt;
     N.kd_full = &h.ctrl.p->kd_full;
+    N.v_half = &h.ctrl.p->v_half;
     N.ld = h.L.ld;
     N.nx = h.L.nx;
     N.ny = h.L.ny;
@@ -899,7 +930,8 @@ static void enqueue_dyn_mixed_fused(Handle& h) {
         return A;
     };
     const int64_t n0 = std::min<int64_t>(5 * (int64_t)h.L.ld, n);
-    k_dyn_predict_nm<<<vblocks4(n0), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, 0, n0, h.ctrl.p, 1);
+    k_dyn_predict_nm<<<vblocks4(n0), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, 0, n0, h.L.ld,
+                                                  h.ctrl.p, 1);
     EQC_CHECK_LAUNCH();
     EQC_CUDA(cudaEventRecord(h.ev_fork, s));
     // fault row
@@ -917,7 +949,7 @@ static void enqueue_dyn_mixed_fused(Handle& h) {
     EQC_CUDA(cudaEventRecord(h.ev_join, h.side_stream));
     // K d off the fault row
     k_dyn_predict_nm<<<vblocks4(n - n0), 256, 0, s>>>(h.d.p, h.v.p, h.a.p, h.F.vPre.p, h.g32.p, h.F.Nf, n0, n,
-                                                      h.ctrl.p, 0);
+                                                      h.L.ld, h.ctrl.p, 0);
     EQC_CHECK_LAUNCH();
     EQC_CUDA(cudaEventRecord(h.ev_fork2, s));
     EQC_CUDA(cudaStreamWaitEvent(h.side_stream2, h.ev_fork2, 0));
@@ -997,6 +1029,15 @@ static void enqueue_dyn(Handle& h, bool graph) {
 }
 
 // One whole time step, ending with the control kernel (Vfmax, regime, next dt).
+void materialize_dyn_state(Handle& h) {
+    if (!h.nm_fused || h.opt.precision != EQC_MIXED) return;
+    k_nm_materialize<<<vblocks(h.L.size()), 256, 0, h.stream>>>(h.ctrl.p, nm_args(h));
+    EQC_CHECK_LAUNCH();
+    count_launch();
+    EQC_CUDA(cudaMemsetAsync(&h.ctrl.p->v_half, 0, sizeof(int), h.stream));   // after every CTA read it
+    if (h.h_ctrl) h.h_ctrl->v_half = 0;
+}
+
 void enqueue_step(Handle& h, int iso, bool graph) {
     // the mixed method's dynamic step advances it and t in its predictor and runs the control in
     // its fault kernel
@@ -1032,7 +1073,7 @@ void destroy_graphs(Handle& h) {
 __global__ void k_step_end(Ctrl* C, double* __restrict__ log_t, double* __restrict__ log_vf,
                            double* __restrict__ log_seis, const int64_t* __restrict__ iSeis, int ns,
                            const double* __restrict__ d, const double* __restrict__ v, const double* __restrict__ a,
-                           int regime, cudaGraphConditionalHandle hw) {
+                           NmEpi N, int regime, cudaGraphConditionalHandle hw) {
     EQC_GRID_WAIT();
     __shared__ int rec;
     const long long it = C->it;
@@ -1046,9 +1087,11 @@ __global__ void k_step_end(Ctrl* C, double* __restrict__ log_t, double* __restri
     if (rec >= 0 && (int)threadIdx.x < ns) {
         const int64_t g = iSeis[threadIdx.x];
         double* o = log_seis + (int64_t)rec * 3 * ns;
+        double vg = v[g], ag = a[g];
+        if (C->v_half && g >= N.ld) nm_state_at(N, g, C->half_dt, &vg, &ag);
         o[threadIdx.x] = d[g];
-        o[ns + threadIdx.x] = v[g];
-        o[2 * ns + threadIdx.x] = a[g];
+        o[ns + threadIdx.x] = vg;
+        o[2 * ns + threadIdx.x] = ag;
     }
     if (threadIdx.x == 0) {
         C->nlog = k + 1;
@@ -1086,7 +1129,7 @@ static StepGraph& batched_graph(Handle& h, int iso) {
         cond_begin(h, cudaGraphCondTypeWhile, hw);
         enqueue_step(h, iso, true);
         k_step_end<<<1, 32, 0, h.stream>>>(h.ctrl.p, h.log_t.p, h.log_vf.p, h.log_seis.p, h.iSeis.p, h.nSeis, h.d.p,
-                                            h.v.p, h.a.p, iso, hw);
+                                            h.v.p, h.a.p, nm_args(h), iso, hw);
         EQC_CHECK_LAUNCH();
         count_launch();
         cond_end(h);
@@ -1229,7 +1272,7 @@ void post_step(Handle& h, int iso, eqc_run_stats& stats, PostBufs& pb, bool logg
     if (!logged && C.it % 10 == 0 && h.nSeis > 0) {
         if (h.rit >= CAP_SEIS) throw Error(EQC_E_CAPACITY, "receiver capacity (190000) exceeded");
         h.rit += 1;
-        k_gather_seis<<<1, 32, 0, s>>>(h.iSeis.p, h.nSeis, h.d.p, h.v.p, h.a.p, h.seis.p);
+        k_gather_seis<<<1, 32, 0, s>>>(h.iSeis.p, h.nSeis, h.d.p, h.v.p, h.a.p, h.seis.p, h.ctrl.p, nm_args(h));
         count_launch();
         EQC_CUDA(cudaMemcpyAsync(seis.data(), h.seis.p, sizeof(double) * 3 * h.nSeis, cudaMemcpyDeviceToHost, s));
         EQC_CUDA(cudaStreamSynchronize(s));
