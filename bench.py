@@ -725,33 +725,51 @@ def bench_learned(args):
 def bench_ensemble(args):
     """The batched ensemble: 64 uneven damage-zone models (120x60 to 480x240 elements, seeded
     parameters) advanced by one CUDA-graph launch per step, mixed precision with the extrapolated
-    guess; compared with the same members stepped one after another with their own graphs.  Under
-    torchrun the members are split across the ranks (shard_members; no exchange), each rank runs
-    its share as one ensemble, and the whole-job value is all ranks' simulated years over the
-    slowest rank's device time (a fixed total of members: strong scaling)."""
-    from eqcycle_gb300 import (EQC_GUESS_EXTRAPOLATE, EQC_MIXED, Ensemble, Solver, ensemble_members,
-                               structured_parameters)
+    guess, or (--ensemble-guess learned) with the learned guess: every member first steps
+    --learn-steps quasi-static steps on its own logging (features, increment) pairs, trains its own
+    network on them on the GPU and then runs with it, the on-device check keeping an increment only
+    where it lowers the residual; compared with the same members stepped one after another with
+    their own graphs.  Under torchrun the members are split across the ranks (shard_members; no
+    exchange), each rank runs its share as one ensemble, and the whole-job value is all ranks'
+    simulated years over the slowest rank's device time (a fixed total of members: strong
+    scaling)."""
+    from eqcycle_gb300 import (EQC_GUESS_EXTRAPOLATE, EQC_GUESS_LEARNED, EQC_MIXED, Ensemble, Solver,
+                               ensemble_members, structured_parameters)
     from eqcycle_gb300.config import shard_members
     rank, ws, dist = _dist()
     device = int(os.environ.get("LOCAL_RANK", "0"))
+    learned = args.ensemble_guess == "learned"
     t0 = time.time()
     cfgs_all = ensemble_members(args.members)
     cfgs = [cfgs_all[k] for k in shard_members(cfgs_all, rank, ws)]
-    solvers, nodes = [], 0
-    for c in cfgs:
+    solvers, nodes, train_s, pairs = [], 0, 0.0, 0
+    for k, c in enumerate(cfgs):
         P = structured_parameters(c)   # element and node data built on the device
-        s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device, guess=EQC_GUESS_EXTRAPOLATE)
+        s = Solver(P, precision=EQC_MIXED, cg_tol=1e-8, device=device,
+                   guess=EQC_GUESS_LEARNED if learned else EQC_GUESS_EXTRAPOLATE)
         s.init(c.V_init)
         s.set_scalar("dt", steady_dt(s, P))
+        if learned:   # the member's own pairs, its own network (no network until it is trained)
+            s.guess_init(k + 1)
+            s.guess_log(args.learn_steps)
+            s.run(args.learn_steps)
+            xin, tgt = s.guess_pairs()
+            t1 = time.time()
+            s.guess_train(xin, tgt, epochs=args.epochs, lr=1e-3, batch=min(256, max(1, len(xin))), seed=k)
+            train_s += time.time() - t1
+            pairs += len(xin)
         solvers.append(s)
         nodes += P.int_.nglob
     setup_s = time.time() - t0
     E = Ensemble(solvers)
     E.run(args.warmup)
     t_start = [s.scalar("t") for s in solvers]
+    gk = lambda key: sum(s.scalar(key) for s in solvers)
+    g0 = (gk("guess_kept"), gk("guess_tried"))
     _barrier(dist)
     stats, ms = E.run(args.steps)
     _barrier(dist)
+    g1 = (gk("guess_kept"), gk("guess_tried"))
     ms_max = _allreduce(dist, ms, _max_op())
     years = _allreduce(dist, sum((st["t"] - t0_) / YR for st, t0_ in zip(stats, t_start)), _sum_op())
     value = years / (ms_max / 3.6e6)
@@ -773,7 +791,12 @@ def bench_ensemble(args):
             "setup_s": setup_s,
             "config": {"workload": f"{len(solvers)} damage-zone models, 120x60 to 480x240 elements, seeded "
                                    f"parameters; one graph launch per ensemble step; mixed precision, "
-                                   f"extrapolated guess"}}
+                                   + ("learned guess (each member's own network, trained on its first "
+                                      f"{args.learn_steps} quasi-static steps)" if learned else "extrapolated guess")}}
+    if learned:
+        line["learned"] = {"pairs_rank0": pairs, "train_s_rank0": train_s,   # the timed steps' guesses
+                           "guess_kept": int(_allreduce(dist, g1[0] - g0[0], _sum_op())),
+                           "guess_tried": int(_allreduce(dist, g1[1] - g0[1], _sum_op()))}
     E.close()
     for s in solvers:
         s.close()
@@ -856,6 +879,10 @@ def main():
     ap.add_argument("--years", type=float, default=0.0, help="--cycle: simulated years (default: the workload's)")
     ap.add_argument("--cycle-budget", type=float, default=600.0, help="--cycle: wall seconds per method")
     ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--ensemble-guess", default="extrapolate", choices=["extrapolate", "learned"],
+                    help="--ensemble: the members' initial guess")
+    ap.add_argument("--learn-steps", type=int, default=60,
+                    help="--ensemble --ensemble-guess learned: logged quasi-static steps per member before training")
     ap.add_argument("--no-graphs", action="store_true",
                     help="headline leg without CUDA graphs (host-driven steps; for per-kernel profiling)")
     ap.add_argument("--pairs", type=int, default=2400, help="--learned: training pairs over 8 seeds")

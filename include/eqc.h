@@ -86,8 +86,10 @@ typedef struct {
     int32_t use_graphs;  /* capture the per-step work in CUDA graphs     */
     int32_t verbose;     /* print "Time (yr) = ..." every 500 steps (main.jl:425-427) */
     /* solver tuning (0 = default) */
-    double reliable_delta;  /* mixed precision: FP64 residual replacement whenever the
-                               recurrence residual fell by this factor (default 1e-3)  */
+    double reliable_delta;  /* mixed precision: a reliable update whenever the recurrence
+                               residual fell by this factor (default 1e-3): r -= K dx with
+                               a double-float apply, b - K x in FP64 for the update that
+                               certifies convergence                                   */
     int32_t mg_degree;      /* Chebyshev smoothing steps on the spectral-element level, pre and
                                post (default 4)                                        */
     int32_t mg_coarse_max;  /* largest coarsest level, solved densely (default 2048 unknowns) */
