@@ -12,6 +12,8 @@ namespace eqc {
 
 int64_t g_launches = 0;
 
+int vec_blocks() { return VEC_BLOCKS; }
+
 // x and y 16-byte aligned; 4-wide chunks on a fixed grid, the n % 4 tail in thread 0
 template <class T>
 __global__ void __launch_bounds__(VEC_THREADS) k_dot(const T* __restrict__ x, const T* __restrict__ y, int64_t n,
@@ -40,13 +42,13 @@ static void check_vec(const void* x, const void* y, int64_t) {
 
 void dot64(Handle& h, const double* x, const double* y, int64_t n, double* out_dev) {
     check_vec(x, y, n);
-    k_dot<double><<<VEC_BLOCKS, VEC_THREADS, 0, h.stream>>>(x, y, n, h.red_part.p, h.red_count.p, out_dev);
+    k_dot<double><<<vec_blocks(), VEC_THREADS, 0, h.stream>>>(x, y, n, h.red_part.p, h.red_count.p, out_dev);
     EQC_CHECK_LAUNCH();
     count_launch();
 }
 void dot32(Handle& h, const float* x, const float* y, int64_t n, double* out_dev) {
     check_vec(x, y, n);
-    k_dot<float><<<VEC_BLOCKS, VEC_THREADS, 0, h.stream>>>(x, y, n, h.red_part.p, h.red_count.p, out_dev);
+    k_dot<float><<<vec_blocks(), VEC_THREADS, 0, h.stream>>>(x, y, n, h.red_part.p, h.red_count.p, out_dev);
     EQC_CHECK_LAUNCH();
     count_launch();
 }

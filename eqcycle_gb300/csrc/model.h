@@ -230,6 +230,7 @@ bool apply_K_epi(const float* x, const ApplyArgs<float>& A, int mode, const OpEp
 bool apply_K_fault32(const float* x, float* y, const ApplyArgs<float>& A, cudaStream_t s);
 
 // blas.cu
+int vec_blocks();   // grid of the vector and reduction kernels
 void dot64(Handle& h, const double* x, const double* y, int64_t n, double* out_dev);
 void dot32(Handle& h, const float* x, const float* y, int64_t n, double* out_dev);
 

@@ -187,7 +187,7 @@ __global__ void k_set_sigma(CGState* S, int mixed) {
     S->sigma = (mixed && nb > 0 && isfinite(nb)) ? ldexp(1.0, -ilogb(nb)) : 1.0;
 }
 
-static inline dim3 vgrid() { return dim3(VEC_BLOCKS); }
+static inline dim3 vgrid() { return dim3(vec_blocks()); }
 
 // ---- device-side control of the CG loop -----------------------------------------------
 // Every control kernel is a single thread: it owns the CGState and is the only caller of

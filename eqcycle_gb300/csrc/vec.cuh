@@ -8,7 +8,10 @@
 
 namespace eqc {
 
-constexpr int VEC_BLOCKS = 8 * 152;   // 8 CTAs of 256 threads per SM of a GB300
+// 3 CTAs of 256 threads per SM of a GB300: the reductions' last-CTA tickets and partials cost
+// less than with 8 per SM, and 4-wide grid-stride loops keep enough loads in flight (dz480
+// quasi-static steps: 73.0 ms for 20 with 8 per SM, 72.6 with 4, 71.9 with 3, 72.1 with 2)
+constexpr int VEC_BLOCKS = 3 * 152;
 constexpr int VEC_THREADS = 256;
 
 __device__ __forceinline__ void ld4(const float* p, float (&a)[4]) {
