@@ -37,14 +37,20 @@ struct NmEpi {
 template <class T>
 struct OpEpi {
     int mode = 0;              // 0: y = t;  1: r = b - t (residual);  2: Chebyshev step, x of the
-                               //    kernel is the direction dold (r, x updated, d' into dnew)
-    const T* b = nullptr;      // mode 1
-    T* r = nullptr;            // modes 1, 2
-    const T* dinv = nullptr;   // mode 2
+                               //    kernel is the direction dold (r, x updated, d' into dnew);
+                               // 3: first Chebyshev step from x, t = A x: r = Dinv (b - t) and
+                               //    d = r / theta into dnew, x += d left pending (x is the
+                               //    operand other CTAs are still reading): the next step adds it
+                               //    (x_pend) or the next reader of x does
+    const T* b = nullptr;      // modes 1, 3
+    T* r = nullptr;            // modes 1-3
+    const T* dinv = nullptr;   // modes 2, 3
     const T* dold = nullptr;
     T* dnew = nullptr;
     T* x = nullptr;
     T c1 = T(0), c2 = T(0);
+    T inv_theta = T(0);        // mode 3
+    bool x_pend = false;       // mode 2: x += dold (the first step's pending direction) first
 };
 
 #if defined(__CUDACC__)
@@ -67,6 +73,14 @@ __device__ __forceinline__ void cheb_step_pt(T& r, T& d, T& x, T t, T dinv, T c1
     r = fma_rn<T>(-dinv, t, r);
     d = fma_rn<T>(c1, d, mul_rn<T>(c2, r));
     x = add_rn<T>(x, d);
+}
+
+// First Chebyshev step from x at one node, t = (A x)_i:  r = Dinv (b - t) ; d = r / theta (the
+// operations of k_cheb_first with x, in its order; its x += d is add_rn(x, d) wherever it lands)
+template <class T>
+__device__ __forceinline__ void cheb_first_rd_pt(T& r, T& d, T b, T t, T dinv, T inv_theta) {
+    r = mul_rn<T>(dinv, sub_rn<T>(b, t));
+    d = mul_rn<T>(r, inv_theta);
 }
 
 // FP32 -> FP64, exact, by integer operations on the bit patterns (GB300 converts to FP64 on its
@@ -158,11 +172,27 @@ __device__ __forceinline__ void epi_store4(const OpEpi<float>& E, float* y, int6
         const float4 b = __ldg(reinterpret_cast<const float4*>(E.b + off));
         *reinterpret_cast<float4*>(E.r + off) =
             make_float4(sub_rn(b.x, t.x), sub_rn(b.y, t.y), sub_rn(b.z, t.z), sub_rn(b.w, t.w));
+    } else if (E.mode == 3) {
+        const float4 b = __ldg(reinterpret_cast<const float4*>(E.b + off));
+        const float4 di = __ldg(reinterpret_cast<const float4*>(E.dinv + off));
+        float4 r, d;
+        cheb_first_rd_pt(r.x, d.x, b.x, t.x, di.x, E.inv_theta);
+        cheb_first_rd_pt(r.y, d.y, b.y, t.y, di.y, E.inv_theta);
+        cheb_first_rd_pt(r.z, d.z, b.z, t.z, di.z, E.inv_theta);
+        cheb_first_rd_pt(r.w, d.w, b.w, t.w, di.w, E.inv_theta);
+        *reinterpret_cast<float4*>(E.r + off) = r;
+        *reinterpret_cast<float4*>(E.dnew + off) = d;
     } else {
         float4 r = *reinterpret_cast<const float4*>(E.r + off);
         float4 x = *reinterpret_cast<const float4*>(E.x + off);
         float4 d = __ldg(reinterpret_cast<const float4*>(E.dold + off));
         const float4 di = __ldg(reinterpret_cast<const float4*>(E.dinv + off));
+        if (E.x_pend) {
+            x.x = add_rn(x.x, d.x);
+            x.y = add_rn(x.y, d.y);
+            x.z = add_rn(x.z, d.z);
+            x.w = add_rn(x.w, d.w);
+        }
         cheb_step_pt(r.x, d.x, x.x, t.x, di.x, E.c1, E.c2);
         cheb_step_pt(r.y, d.y, x.y, t.y, di.y, E.c1, E.c2);
         cheb_step_pt(r.z, d.z, x.z, t.z, di.z, E.c1, E.c2);
@@ -180,8 +210,14 @@ __device__ __forceinline__ void epi_store1(const OpEpi<T>& E, T* y, int64_t i, T
         y[i] = t;
     } else if (E.mode == 1) {
         E.r[i] = sub_rn<T>(E.b[i], t);
+    } else if (E.mode == 3) {
+        T r, d;
+        cheb_first_rd_pt<T>(r, d, E.b[i], t, E.dinv[i], E.inv_theta);
+        E.r[i] = r;
+        E.dnew[i] = d;
     } else {
         T r = E.r[i], d = E.dold[i], x = E.x[i];
+        if (E.x_pend) x = add_rn<T>(x, d);
         cheb_step_pt<T>(r, d, x, t, E.dinv[i], E.c1, E.c2);
         E.r[i] = r;
         E.x[i] = x;

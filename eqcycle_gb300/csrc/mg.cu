@@ -19,18 +19,22 @@ __global__ void k_stencil(const T* __restrict__ A, const T* __restrict__ x, T* _
         epi_store1(E, y, i, stencil_pt<T>(A, x, cx, cy, N, i, LdPlain()));
 }
 
-// xf[fine] += sum_{a,b} wx_a wy_b xc[coarse]   (fine rows >= 1)
+// xf[fine] += sum_{a,b} wx_a wy_b xc[coarse]   (fine rows >= 1); xc + pend where the coarse
+// level's post-smoothing left its first step's direction pending (pend non-null)
 template <class T>
 __global__ void k_prolong_add(const T* __restrict__ xc, T* __restrict__ xf, int nfx, int nfy, int ldf, int ldc,
                               const int* __restrict__ px, const int* __restrict__ py, const T* __restrict__ wx,
-                              const T* __restrict__ wy) {
+                              const T* __restrict__ wy, const T* __restrict__ pend) {
     EQC_GRID_WAIT();
     const int64_t N = (int64_t)nfx * nfy;
+    LdPend ld;
+    ld.base = xc;
+    ld.pend = pend;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % nfx), iy = (int)(i / nfx);
         if (iy == 0) continue;
         T* o = xf + (int64_t)iy * ldf + ix;
-        *o = add_rn<T>(*o, prolong_pt<T>(xc, ldc, px, py, wx, wy, ix, iy, LdPlain()));
+        *o = add_rn<T>(*o, prolong_pt<T>(xc, ldc, px, py, wx, wy, ix, iy, ld));
     }
 }
 
@@ -62,17 +66,21 @@ struct GllW {
 // xf[iy, 4ex + k] += P0 xc  for node rows iy >= 1; one thread per (element column, node row),
 // the thread of the last element column also takes the lattice's last node.
 template <class T>
-__global__ void k_prolong_sem(const T* __restrict__ xc, T* __restrict__ xf, Layout L, int ldc, GllW<T> w) {
+__global__ void k_prolong_sem(const T* __restrict__ xc, T* __restrict__ xf, Layout L, int ldc, GllW<T> w,
+                              const T* __restrict__ pend) {
     EQC_GRID_WAIT();
     const int ex = blockIdx.x * blockDim.x + threadIdx.x;
     const int iy = blockIdx.y + 1;
     if (ex >= L.NelX || iy >= L.ny) return;
+    LdPend ld;
+    ld.base = xc;
+    ld.pend = pend;
     const int ey = min(iy >> 2, L.NelY - 1), ky = iy - 4 * ey;
     const T wyl = ky == 4 ? T(0) : w.lo[ky], wyh = ky == 4 ? T(1) : w.hi[ky];
     const T* c0 = xc + (int64_t)ey * ldc + ex;
     const T* c1 = c0 + ldc;
-    const T a0 = wyl * c0[0] + wyh * c1[0];       // vertex column ex
-    const T a1 = wyl * c0[1] + wyh * c1[1];       // vertex column ex + 1
+    const T a0 = wyl * ld(c0) + wyh * ld(c1);           // vertex column ex
+    const T a1 = wyl * ld(c0 + 1) + wyh * ld(c1 + 1);   // vertex column ex + 1
     T* row = xf + (int64_t)iy * L.ld + 4 * ex;
 #pragma unroll
     for (int k = 0; k < 4; ++k) row[k] += w.lo[k] * a0 + w.hi[k] * a1;
@@ -131,6 +139,14 @@ __global__ void k_cheb_step(T* __restrict__ x, T* __restrict__ r, T* __restrict_
         d[i] = di;
         x[i] = xi;
     }
+}
+// x += d: a post-smoothing's pending first-step direction (OpEpi mode 3) with no later reader
+// to add it
+template <class T>
+__global__ void k_add_pend(T* __restrict__ x, const T* __restrict__ d, int64_t n) {
+    EQC_GRID_WAIT();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = add_rn<T>(x[i], d[i]);
 }
 // r = b - t
 template <class T>
@@ -247,10 +263,6 @@ static int64_t level_size(Handle& h, int l) {
     return l == 0 ? h.L.size() : (int64_t)h.mg->lev[l - 1].cx * h.mg->lev[l - 1].cy;
 }
 
-// Chebyshev smoothing of A_l x = b (deg steps), x = 0 initially when !with_x.  first_done: the
-// first step (from x = 0) already ran inside the restriction that produced b.  Later steps run
-// fused into the operator (r, x updated in place, the direction alternating between the d and t
-// work vectors) when the level's operator kernel has the epilogue.
 // The Chebyshev smoother's coefficients on level l (0: the spectral-element level): 1/theta of
 // the first step and (c1[k], c2[k]) of steps k = 1..deg-1.
 static void cheb_coeffs(const MGHier& m, int l, int deg, double* inv_theta, double* c1, double* c2) {
@@ -268,8 +280,14 @@ static void cheb_coeffs(const MGHier& m, int l, int deg, double* inv_theta, doub
     }
 }
 
+// Chebyshev smoothing of A_l x = b (deg steps), x = 0 initially when !with_x.  first_done: the
+// first step (from x = 0) already ran inside the restriction that produced b.  Steps run fused
+// into the operator (r, x updated in place, the direction alternating between the d and t work
+// vectors) when the level's operator kernel has the epilogue; the first step from x then leaves
+// x += d pending (OpEpi mode 3) for the second step, or, with one step, returns d for the
+// caller's next reader of x to add (null: x is complete).
 template <class T>
-static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x, bool first_done = false) {
+static const T* chebyshev(Handle& h, int l, T* x, const T* b, bool with_x, bool first_done = false) {
     MGHier& m = *h.mg;
     MGWork& w = m.work[l];
     const int64_t n = level_size(h, l);
@@ -281,10 +299,22 @@ static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x, bool firs
     T* r = Sel<T>::r(w);
     T* d = Sel<T>::d(w);
     T* t = Sel<T>::t(w);
+    bool pend = false;
     if (!first_done) {
-        if (with_x) level_apply<T>(h, l, x, t);
-        k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)inv_theta, with_x ? 1 : 0);
-        count_launch();
+        OpEpi<T> E;
+        E.mode = 3;
+        E.b = b;
+        E.r = r;
+        E.dinv = Dinv;
+        E.dnew = d;
+        E.inv_theta = (T)inv_theta;
+        if (with_x && epi_apply(h, l, x, E)) {
+            pend = true;
+        } else {
+            if (with_x) level_apply<T>(h, l, x, t);
+            k_cheb_first<T><<<vb(n), 256, 0, h.stream>>>(x, r, d, b, t, Dinv, n, (T)inv_theta, with_x ? 1 : 0);
+            count_launch();
+        }
     }
     T* dcur = d;
     T* dnext = t;
@@ -299,15 +329,22 @@ static void chebyshev(Handle& h, int l, T* x, const T* b, bool with_x, bool firs
         E.x = x;
         E.c1 = c1;
         E.c2 = c2;
+        E.x_pend = pend;
         if (epi_apply(h, l, dcur, E)) {
             std::swap(dcur, dnext);
         } else {
+            if (pend) {
+                k_add_pend<T><<<vb(n), 256, 0, h.stream>>>(x, dcur, n);
+                count_launch();
+            }
             level_apply<T>(h, l, dcur, t);
             k_cheb_step<T><<<vb(n), 256, 0, h.stream>>>(x, r, dcur, t, Dinv, n, c1, c2);
             count_launch();
         }
+        pend = false;
     }
     EQC_CHECK_LAUNCH();
+    return pend ? dcur : nullptr;
 }
 
 // 1 / theta of level l's Chebyshev interval (as chebyshev() computes it)
@@ -318,8 +355,9 @@ static double cheb_inv_theta(const MGHier& m, int l) {
 }
 
 // first_done: the restriction that produced b already took level l's first smoothing step.
+// Returns the post-smoothing's pending direction (chebyshev), null when x is complete.
 template <class T>
-static void vcycle(Handle& h, int l, T* x, const T* b, bool first_done = false) {
+static const T* vcycle(Handle& h, int l, T* x, const T* b, bool first_done = false) {
     MGHier& m = *h.mg;
     const int L = (int)m.lev.size();
     if (l == L) {  // coarsest: dense solve on rows >= 1
@@ -330,11 +368,11 @@ static void vcycle(Handle& h, int l, T* x, const T* b, bool first_done = false) 
         EQC_CHECK_LAUNCH();
         count_launch();
         (void)n;
-        return;
+        return nullptr;
     }
     MGWork& w = m.work[l];
     const int64_t n = level_size(h, l);
-    chebyshev<T>(h, l, x, b, false, first_done);
+    chebyshev<T>(h, l, x, b, false, first_done);   // from x = 0: nothing pending
     // residual r = b - A x, fused into the operator where it has the epilogue
     T* t = Sel<T>::t(w);
     T* r = Sel<T>::r(w);
@@ -370,29 +408,41 @@ static void vcycle(Handle& h, int l, T* x, const T* b, bool first_done = false) 
                                                                            tr.riy.p, Sel<T>::rwy(tr), F);
     }
     count_launch();
-    vcycle<T>(h, l + 1, xc, bc, fuse);
+    const T* pc = vcycle<T>(h, l + 1, xc, bc, fuse);
     if (l == 0) {
-        k_prolong_sem<T><<<dim3((h.L.NelX + 127) / 128, h.L.ny - 1), 128, 0, h.stream>>>(xc, x, h.L, tr.ldc, gw);
+        k_prolong_sem<T><<<dim3((h.L.NelX + 127) / 128, h.L.ny - 1), 128, 0, h.stream>>>(xc, x, h.L, tr.ldc, gw, pc);
     } else {
         k_prolong_add<T><<<vb((int64_t)tr.nfx * tr.nfy), 256, 0, h.stream>>>(xc, x, tr.nfx, tr.nfy, tr.ldf, tr.ldc,
                                                                              tr.px.p, tr.py.p, Sel<T>::wx(tr),
-                                                                             Sel<T>::wy(tr));
+                                                                             Sel<T>::wy(tr), pc);
     }
     count_launch();
     EQC_CHECK_LAUNCH();
-    chebyshev<T>(h, l, x, b, true);
+    return chebyshev<T>(h, l, x, b, true);
+}
+
+// The whole V-cycle on level 0 with any pending direction added to x.
+template <class T>
+static void vcycle0(Handle& h, T* x, const T* b) {
+    const T* p = vcycle<T>(h, 0, x, b);
+    if (p) {
+        const int64_t n = level_size(h, 0);
+        k_add_pend<T><<<vb(n), 256, 0, h.stream>>>(x, p, n);
+        EQC_CHECK_LAUNCH();
+        count_launch();
+    }
 }
 
 // z = M^{-1} r for the CG: r, z are the interior slices (rows >= 1) of level-0 vectors.
 void mg_apply64(Handle& h, const double* r, double* z) {
     if (!h.mg) throw Error(EQC_E_STATE, "multigrid not built");
     const int64_t ld = h.L.ld;
-    vcycle<double>(h, 0, z - ld, r - ld);
+    vcycle0<double>(h, z - ld, r - ld);
 }
 void mg_apply32(Handle& h, const float* r, float* z) {
     if (!h.mg) throw Error(EQC_E_STATE, "multigrid not built");
     const int64_t ld = h.L.ld;
-    vcycle<float>(h, 0, z - ld, r - ld);
+    vcycle0<float>(h, z - ld, r - ld);
 }
 
 // ------------------------------------------------------------------ setup

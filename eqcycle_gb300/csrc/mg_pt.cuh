@@ -15,6 +15,18 @@ struct LdPlain {
     template <class T> __device__ __forceinline__ T operator()(const T* p) const { return *p; }
 };
 
+// A coarse level's correction x read with its post-smoothing's pending first-step direction
+// added (OpEpi mode 3): x + pend at the same offset from base, rounded as k_cheb_first rounds it.
+struct LdPend {
+    const void* base = nullptr;
+    const void* pend = nullptr;   // null: plain loads
+    template <class T> __device__ __forceinline__ T operator()(const T* p) const {
+        const T v = *p;
+        if (!pend) return v;
+        return add_rn<T>(v, static_cast<const T*>(pend)[p - static_cast<const T*>(base)]);
+    }
+};
+
 // The coarse level's first Chebyshev step from x = 0, fused into the restriction that produces
 // its right-hand side (k_cheb_first with with_x = 0): r = Dinv b ; d = r / theta ; x = d.
 template <class T>
@@ -101,7 +113,7 @@ __device__ __forceinline__ void cheb_first_step_pt(T* x, T* r, T* d, const T* b,
     x[i] = with_x ? add_rn<T>(ld(x + i), di) : di;
 }
 
-// The epilogue of a stencil apply at point i (OpEpi modes 0-2), with the vectors it reads
+// The epilogue of a stencil apply at point i (OpEpi modes 0-3), with the vectors it reads
 // loaded through ld.
 template <class T, class Ld>
 __device__ __forceinline__ void epi_store1_ld(const OpEpi<T>& E, T* y, int64_t i, T t, Ld ld) {
@@ -109,8 +121,14 @@ __device__ __forceinline__ void epi_store1_ld(const OpEpi<T>& E, T* y, int64_t i
         y[i] = t;
     } else if (E.mode == 1) {
         E.r[i] = sub_rn<T>(ld(E.b + i), t);
+    } else if (E.mode == 3) {
+        T r, d;
+        cheb_first_rd_pt<T>(r, d, ld(E.b + i), t, E.dinv[i], E.inv_theta);
+        E.r[i] = r;
+        E.dnew[i] = d;
     } else {
         T r = ld(E.r + i), d = ld(E.dold + i), x = ld(E.x + i);
+        if (E.x_pend) x = add_rn<T>(x, d);
         cheb_step_pt<T>(r, d, x, t, E.dinv[i], E.c1, E.c2);
         E.r[i] = r;
         E.x[i] = x;
