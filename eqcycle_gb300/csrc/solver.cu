@@ -68,11 +68,23 @@ __global__ void __launch_bounds__(VEC_THREADS) k_pupdate(const T* __restrict__ z
     }
 }
 
-// x += alpha u ; r -= alpha q ; S_RR = r.r   (alpha = rho / (u.q))
+// The update decision (cg_check_a) run by the last CTA of k_xr_update (on = 0: not run), and the
+// loop's condition for an iteration without an update (with one, k_cg_check_b in the update's
+// body sets it again): without an update the loop goes on unless the residual is not finite.
+struct CheckA {
+    int on = 0, use_cond = 0;   // on: 1 the mixed iteration's decision, 2 the FP64 iteration's check
+    double delta = 0.0;
+    cudaGraphConditionalHandle hi = 0, hw = 0;
+};
+__device__ __forceinline__ int cg_check_a(CGState* S, double delta);
+__device__ __forceinline__ int cg_check64(CGState* S);
+
+// x += alpha u ; r -= alpha q ; S_RR = r.r   (alpha = rho / (u.q)); then the update decision
+// (ck.on: S is the CGState)
 template <class TX, class T>
 __global__ void __launch_bounds__(VEC_THREADS) k_xr_update(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ u,
                                                            const T* __restrict__ q, int64_t n, double* part,
-                                                           unsigned* count, double* S) {
+                                                           unsigned* count, double* S, CheckA ck) {
     EQC_GRID_WAIT();
     __shared__ double sh[32];
     const double alpha = S[S_RHO] / S[S_PQ];
@@ -96,7 +108,20 @@ __global__ void __launch_bounds__(VEC_THREADS) k_xr_update(TX* __restrict__ x, T
         st4(r + i, rr);
     }
     const double s = block_sum(acc.value(), sh);
-    finish_reduction(s, part, count, sh, [&](double t) { S[S_RR] = t; });
+    finish_reduction(s, part, count, sh, [&](double t) {
+        S[S_RR] = t;
+        CGState* cs = reinterpret_cast<CGState*>(S);
+        if (ck.on == 1) {
+            const int need = cg_check_a(cs, ck.delta);
+            if (ck.use_cond) {
+                cudaGraphSetConditional(ck.hi, need ? 1u : 0u);
+                cudaGraphSetConditional(ck.hw, cs->done == 0 ? 1u : 0u);
+            }
+        } else if (ck.on == 2) {
+            const int st = cg_check64(cs);
+            if (ck.use_cond) cudaGraphSetConditional(ck.hw, st == 0 ? 1u : 0u);
+        }
+    });
 }
 
 template <class T>
@@ -217,20 +242,18 @@ __global__ void k_cg_init(CGState* S, double tol, int maxit, int rule, int incr_
 }
 
 // End of an FP64 iteration: the loop goes on until ||r|| <= reltol or maxit.
-__global__ void k_cg_check(CGState* S, cudaGraphConditionalHandle hw, int use_cond) {
-    EQC_GRID_WAIT();
+__device__ __forceinline__ int cg_check64(CGState* S) {
     S->it += 1;
     const double r = sqrt(S->rr) / S->sigma;
     S->res = r;
     const int st = !isfinite(r) ? 3 : (r <= S->reltol ? 1 : (S->it >= S->maxit ? 2 : 0));
     S->done = st;
-    if (use_cond) cudaGraphSetConditional(hw, st == 0 ? 1u : 0u);
+    return st;
 }
 
 // Mixed precision, after the FP32 recurrences: decide whether a reliable update is due
 // (the recurrence residual fell by `delta` since the last one, or the loop would stop).
-__global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandle hi, int use_cond) {
-    EQC_GRID_WAIT();
+__device__ __forceinline__ int cg_check_a(CGState* S, double delta) {
     S->it += 1;
     S->restart = 0;   // consumed by this iteration's direction update
     const double rs = sqrt(S->rr) / S->sigma;
@@ -245,7 +268,7 @@ __global__ void k_cg_check_a(CGState* S, double delta, cudaGraphConditionalHandl
     S->need_update = need;
     // a certifying update (the loop would stop) recomputes b - K x in FP64
     S->upd_incr = (need && rs > S->reltol && S->it < S->maxit && S->incr_ok) ? 1 : 0;
-    if (use_cond) cudaGraphSetConditional(hi, need ? 1u : 0u);
+    return need;
 }
 
 // Mixed precision, end of the iteration: take the FP64 residual of a reliable update and
@@ -459,15 +482,20 @@ static void iter_fp64(Handle& h, cudaGraphConditionalHandle hw, int use_cond) {
     k_pupdate<double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho, &S->restart);
     apply_K<double>(h.p64.p, h.q64.p, args64(h), 1.0, 1, h.stream);
     dot64(h, u, q, n, &S->pq);
+    CheckA ck;
+    ck.on = 2;
+    ck.use_cond = use_cond;
+    ck.hw = hw;
     k_xr_update<double, double><<<vgrid(), VEC_THREADS, 0, h.stream>>>(x, r, u, q, n, h.red_part.p, h.red_count.p,
-                                                                       &S->rho);
-    k_cg_check<<<1, 1, 0, h.stream>>>(S, hw, use_cond);
+                                                                       &S->rho, ck);
     EQC_CHECK_LAUNCH();
-    count_launch(4);
+    count_launch(3);
 }
 
-// Mixed precision: FP32 recurrences of one iteration, ending with the update decision.
-static void iter_mixed_a(Handle& h, double delta, cudaGraphConditionalHandle hi, int use_cond) {
+// Mixed precision: FP32 recurrences of one iteration, ending with the update decision (hi) and,
+// for an iteration without an update, the loop's condition (hw).
+static void iter_mixed_a(Handle& h, double delta, cudaGraphConditionalHandle hi, cudaGraphConditionalHandle hw,
+                         int use_cond) {
     const Layout& L = h.L;
     const int64_t ld = L.ld, n = L.size() - ld;
     CGState* S = h.cg.p;
@@ -481,11 +509,16 @@ static void iter_mixed_a(Handle& h, double delta, cudaGraphConditionalHandle hi,
     k_pupdate<float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(z, u, n, &S->rho, &S->restart);
     apply_K<float>(h.p32.p, h.q32.p, args32(h), 1.0f, 1, h.stream);
     dot32(h, u, q, n, &S->pq);
+    CheckA ck;
+    ck.on = 1;
+    ck.use_cond = use_cond;
+    ck.delta = delta;
+    ck.hi = hi;
+    ck.hw = hw;
     k_xr_update<float, float><<<vgrid(), VEC_THREADS, 0, h.stream>>>(y, r, u, q, n, h.red_part.p, h.red_count.p,
-                                                                     &S->rho);
-    k_cg_check_a<<<1, 1, 0, h.stream>>>(S, delta, hi, use_cond);
+                                                                     &S->rho, ck);
     EQC_CHECK_LAUNCH();
-    count_launch(4);
+    count_launch(3);
 }
 
 // Reliable update: x += y ; r = b - K_II x in FP64 ; r32 = r ; S->rr = ||r||^2.
@@ -578,17 +611,16 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry, con
         cond_begin(h, cudaGraphCondTypeWhile, hw);
         if (mixed) {
             const cudaGraphConditionalHandle hi = cond_handle(h);
-            iter_mixed_a(h, delta, hi, 1);
+            iter_mixed_a(h, delta, hi, hw, 1);
             const int64_t t1 = capture_tally();
             cond_begin(h, cudaGraphCondTypeIf, hi);
             update_mixed(h);
-            cond_end(h);
-            const int64_t t2 = capture_tally();
             k_cg_check_b<<<1, 1, 0, h.stream>>>(S, h.ctrl.p, hw, 1);
             count_launch();
+            cond_end(h);
             if (h.capturing) {
-                h.capturing->k_update = t2 - t1;
-                h.capturing->k_iter = (t1 - t0) + (capture_tally() - t2);
+                h.capturing->k_update = capture_tally() - t1;
+                h.capturing->k_iter = t1 - t0;
                 h.capturing->k_bodies += capture_tally() - t0;
             }
         } else {
@@ -605,11 +637,13 @@ void enqueue_solve(Handle& h, double tol, int maxit, bool graph, bool carry, con
         const CGState* hs = &read_cg(h);
         while (hs->done == 0) {
             if (mixed) {
-                iter_mixed_a(h, delta, 0, 0);
+                iter_mixed_a(h, delta, 0, 0, 0);
                 hs = &read_cg(h);
-                if (hs->need_update) update_mixed(h);
-                k_cg_check_b<<<1, 1, 0, h.stream>>>(S, h.ctrl.p, 0, 0);
-                count_launch();
+                if (hs->need_update) {
+                    update_mixed(h);
+                    k_cg_check_b<<<1, 1, 0, h.stream>>>(S, h.ctrl.p, 0, 0);
+                    count_launch();
+                }
             } else {
                 iter_fp64(h, 0, 0);
             }
