@@ -177,6 +177,60 @@ __global__ void __launch_bounds__(256) k_apply(const T* __restrict__ x, T* __res
 // those carries in a fixed order (deterministic, no atomics).  Elements outside the mesh
 // act as W = 0, so the one extra CTA row/column that owns the last node line needs no
 // special case.
+// Even-odd form of the 5-point line contractions (the GLL derivative matrix is centro-
+// antisymmetric, D(4-p, 4-k) = -D(p, k)): with e_m = v_m + v_(4-m), o_m = v_m - v_(4-m),
+//   s_p, s_(4-p) = P +- Q,  P = sum_m a_pm o_m,  Q = sum_m b_pm e_m + g_p v_2   (p = 0, 1)
+//   s_2 = sum_m d_m o_m,    a = (D(p,m) - D(p,4-m)) / 2, b = (D(p,m) + D(p,4-m)) / 2, g = D(p,2),
+// 20 operations instead of 25 multiply-adds (Solomonoff's even-odd decomposition of spectral
+// differentiation).  EO[0] holds the coefficients of s_p = sum_k H(k,p) v_k (the first
+// contraction of a line), EO[1] those of o_i = sum_p H(i,p) s_p (the second).
+struct EOCoef {
+    float a[2][2], b[2][2], g[2], d[2];
+};
+struct EOCoef64 {   // the same coefficients for the FP64 kernels
+    double a[2][2], b[2][2], g[2], d[2];
+};
+__constant__ EOCoef cEO[2];
+__constant__ EOCoef64 cEO64[2];
+__constant__ int cEO_ok;   // H is centro-antisymmetric (else the full contractions are used)
+
+__device__ __forceinline__ void eo5(const float (&v)[5], float (&s)[5], const EOCoef& c) {
+    const float e0 = v[0] + v[4], e1 = v[1] + v[3], o0 = v[0] - v[4], o1 = v[1] - v[3];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+        const float P = fmaf(c.a[p][1], o1, c.a[p][0] * o0);
+        const float Q = fmaf(c.g[p], v[2], fmaf(c.b[p][1], e1, c.b[p][0] * e0));
+        s[p] = P + Q;
+        s[4 - p] = P - Q;
+    }
+    s[2] = fmaf(c.d[1], o1, c.d[0] * o0);
+}
+
+__device__ __forceinline__ void eo5(const double (&v)[5], double (&s)[5], const EOCoef64& c) {
+    const double e0 = v[0] + v[4], e1 = v[1] + v[3], o0 = v[0] - v[4], o1 = v[1] - v[3];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+        const double P = fma(c.a[p][1], o1, c.a[p][0] * o0);
+        const double Q = fma(c.g[p], v[2], fma(c.b[p][1], e1, c.b[p][0] * e0));
+        s[p] = P + Q;
+        s[4 - p] = P - Q;
+    }
+    s[2] = fma(c.d[1], o1, c.d[0] * o0);
+}
+
+// The FP64 node-line kernels take the even-odd contractions where H allows (FP64 issue rate
+// bounds them on GB300: 20 operations per contraction instead of 25); the FP32 ones keep the
+// full form.
+template <class T> __device__ __forceinline__ bool eo_lines() { return false; }
+template <> __device__ __forceinline__ bool eo_lines<double>() { return cEO_ok != 0; }
+template <class T> struct EOSel;
+template <> struct EOSel<float> {
+    static __device__ __forceinline__ const EOCoef& c(int k) { return cEO[k]; }
+};
+template <> struct EOSel<double> {
+    static __device__ __forceinline__ const EOCoef64& c(int k) { return cEO64[k]; }
+};
+
 // Line items and output pass shared by both full-apply kernels.  us: node tile with row
 // pitch UP; ws: element tile, element stride WP, EX elements per row.
 template <class T, int TEX, int TEY, int NT, int UP, int WP>
@@ -196,21 +250,30 @@ __device__ __forceinline__ void lines_compute(const T* __restrict__ us, const T*
         T u[5], s[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k) u[k] = ul[k];
-#pragma unroll
-        for (int p = 0; p < 5; ++p) {
-            T acc = T(0);
-#pragma unroll
-            for (int k = 0; k < 5; ++k) acc += Hc<T>(k, p) * u[k];
-            const T wr = (j == 0) ? w1[p] + w0[p] : w1[p];
-            s[p] = wr * acc;
-        }
         T o[5];
+        if (eo_lines<T>()) {
+            eo5(u, s, EOSel<T>::c(0));
 #pragma unroll
-        for (int i = 0; i < 5; ++i) {
-            T acc = T(0);
+            for (int p = 0; p < 5; ++p) s[p] *= (j == 0) ? w1[p] + w0[p] : w1[p];
+            eo5(s, o, EOSel<T>::c(1));
 #pragma unroll
-            for (int p = 0; p < 5; ++p) acc += Hc<T>(i, p) * s[p];
-            o[i] = A.c1 * acc;
+            for (int i = 0; i < 5; ++i) o[i] = A.c1 * o[i];
+        } else {
+#pragma unroll
+            for (int p = 0; p < 5; ++p) {
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) acc += Hc<T>(k, p) * u[k];
+                const T wr = (j == 0) ? w1[p] + w0[p] : w1[p];
+                s[p] = wr * acc;
+            }
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                T acc = T(0);
+#pragma unroll
+                for (int p = 0; p < 5; ++p) acc += Hc<T>(i, p) * s[p];
+                o[i] = A.c1 * acc;
+            }
         }
         if (c > 0) {
 #pragma unroll
@@ -229,21 +292,30 @@ __device__ __forceinline__ void lines_compute(const T* __restrict__ us, const T*
         T u[5], s[5];
 #pragma unroll
         for (int l = 0; l < 5; ++l) u[l] = ul[l * UP];
-#pragma unroll
-        for (int p = 0; p < 5; ++p) {
-            T acc = T(0);
-#pragma unroll
-            for (int l = 0; l < 5; ++l) acc += u[l] * Hc<T>(l, p);
-            const T wc = (i == 0) ? w1[5 * p] + w0[5 * p] : w1[5 * p];
-            s[p] = wc * acc;
-        }
         T o[5];
+        if (eo_lines<T>()) {
+            eo5(u, s, EOSel<T>::c(0));
 #pragma unroll
-        for (int jj = 0; jj < 5; ++jj) {
-            T acc = T(0);
+            for (int p = 0; p < 5; ++p) s[p] *= (i == 0) ? w1[5 * p] + w0[5 * p] : w1[5 * p];
+            eo5(s, o, EOSel<T>::c(1));
 #pragma unroll
-            for (int p = 0; p < 5; ++p) acc += s[p] * Hc<T>(jj, p);
-            o[jj] = A.c2 * acc;
+            for (int jj = 0; jj < 5; ++jj) o[jj] = A.c2 * o[jj];
+        } else {
+#pragma unroll
+            for (int p = 0; p < 5; ++p) {
+                T acc = T(0);
+#pragma unroll
+                for (int l = 0; l < 5; ++l) acc += u[l] * Hc<T>(l, p);
+                const T wc = (i == 0) ? w1[5 * p] + w0[5 * p] : w1[5 * p];
+                s[p] = wc * acc;
+            }
+#pragma unroll
+            for (int jj = 0; jj < 5; ++jj) {
+                T acc = T(0);
+#pragma unroll
+                for (int p = 0; p < 5; ++p) acc += s[p] * Hc<T>(jj, p);
+                o[jj] = A.c2 * acc;
+            }
         }
         if (er > 0) {
 #pragma unroll
@@ -546,31 +618,6 @@ __device__ __forceinline__ void rows_lines_t(const float (&u)[5][5], const WAcc&
             }
         }
     }
-}
-
-// Even-odd form of the 5-point line contractions (the GLL derivative matrix is centro-
-// antisymmetric, D(4-p, 4-k) = -D(p, k)): with e_m = v_m + v_(4-m), o_m = v_m - v_(4-m),
-//   s_p, s_(4-p) = P +- Q,  P = sum_m a_pm o_m,  Q = sum_m b_pm e_m + g_p v_2   (p = 0, 1)
-//   s_2 = sum_m d_m o_m,    a = (D(p,m) - D(p,4-m)) / 2, b = (D(p,m) + D(p,4-m)) / 2, g = D(p,2),
-// 20 operations instead of 25 multiply-adds (Solomonoff's even-odd decomposition of spectral
-// differentiation).  EO[0] holds the coefficients of s_p = sum_k H(k,p) v_k (the first
-// contraction of a line), EO[1] those of o_i = sum_p H(i,p) s_p (the second).
-struct EOCoef {
-    float a[2][2], b[2][2], g[2], d[2];
-};
-__constant__ EOCoef cEO[2];
-__constant__ int cEO_ok;   // H is centro-antisymmetric (else the full contractions are used)
-
-__device__ __forceinline__ void eo5(const float (&v)[5], float (&s)[5], const EOCoef& c) {
-    const float e0 = v[0] + v[4], e1 = v[1] + v[3], o0 = v[0] - v[4], o1 = v[1] - v[3];
-#pragma unroll
-    for (int p = 0; p < 2; ++p) {
-        const float P = fmaf(c.a[p][1], o1, c.a[p][0] * o0);
-        const float Q = fmaf(c.g[p], v[2], fmaf(c.b[p][1], e1, c.b[p][0] * e0));
-        s[p] = P + Q;
-        s[4 - p] = P - Q;
-    }
-    s[2] = fmaf(c.d[1], o1, c.d[0] * o0);
 }
 
 __device__ __forceinline__ void rows_lines_eo(const float (&u)[5][5], const float (&W)[28], float c1, float c2,
@@ -1060,8 +1107,21 @@ void set_H(const double* H, cudaStream_t s) {
                 c[t].d[p] = (float)M(2, p);
             }
         }
+        EOCoef64 c64[2];
+        for (int t = 0; t < 2; ++t) {
+            auto M = [&](int r, int q) { return t == 0 ? D1(r, q) : D2(r, q); };
+            for (int p = 0; p < 2; ++p) {
+                for (int m = 0; m < 2; ++m) {
+                    c64[t].a[p][m] = 0.5 * (M(p, m) - M(p, 4 - m));
+                    c64[t].b[p][m] = 0.5 * (M(p, m) + M(p, 4 - m));
+                }
+                c64[t].g[p] = M(p, 2);
+                c64[t].d[p] = M(2, p);
+            }
+        }
         const int ok = asym <= 1e-12 * hmax ? 1 : 0;
         EQC_CUDA(cudaMemcpyToSymbolAsync(cEO, c, sizeof(c), 0, cudaMemcpyHostToDevice, s));
+        EQC_CUDA(cudaMemcpyToSymbolAsync(cEO64, c64, sizeof(c64), 0, cudaMemcpyHostToDevice, s));
         EQC_CUDA(cudaMemcpyToSymbolAsync(cEO_ok, &ok, sizeof(int), 0, cudaMemcpyHostToDevice, s));
     }
     EQC_CUDA(cudaStreamSynchronize(s));
