@@ -447,6 +447,31 @@ static void from_layout(const Handle& h, const std::vector<double>& lay, double*
     }, 1);
 }
 
+// The same maps on the device, for the state transfers of eqc_get_state / eqc_set_state: the
+// field crosses PCIe / C2C in the reference numbering and is permuted by a kernel (the padding
+// entries of the layout are zero).
+__global__ void k_ref_to_layout(const double* __restrict__ ref, const int* __restrict__ map, int64_t n,
+                                double* __restrict__ lay) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+        lay[map[g]] = ref[g];
+}
+__global__ void k_layout_to_ref(const double* __restrict__ lay, const int* __restrict__ map, int64_t n,
+                                double* __restrict__ ref) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+        ref[g] = lay[map[g]];
+}
+static void ensure_ref_maps(Handle& h) {
+    if (h.d_ref2lay.p) return;
+    fail_if(h.L.size() > INT32_MAX, "node layout too large for 32-bit indices");
+    std::vector<int> m32(h.nglob);
+    for (int64_t g = 0; g < h.nglob; ++g) m32[g] = (int)h.ref2lay[g];
+    h.d_ref2lay.alloc(h.nglob);
+    h.d_ref2lay.upload(m32.data(), m32.size(), h.stream);
+    h.ref_stage.alloc(h.nglob);
+    EQC_CUDA(cudaStreamSynchronize(h.stream));
+}
+static int ref_blocks(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 8 * 152); }
+
 static thread_local std::string g_create_err;
 void set_thread_error(const std::string& msg) { g_create_err = msg; }
 
@@ -627,13 +652,14 @@ eqc_status eqc_get_state(eqc_handle* H, const char* name, double* out) {
         if (b == &h.v || b == &h.a) materialize_dyn_state(h);
         if (fault) {
             b->download(out, h.F.Nf, h.stream);
-            EQC_CUDA(cudaStreamSynchronize(h.stream));
         } else {
-            std::vector<double> l(h.L.size());
-            b->download(l.data(), l.size(), h.stream);
-            EQC_CUDA(cudaStreamSynchronize(h.stream));
-            from_layout(h, l, out);
+            ensure_ref_maps(h);
+            k_layout_to_ref<<<ref_blocks(h.nglob), 256, 0, h.stream>>>(b->p, h.d_ref2lay.p, h.nglob, h.ref_stage.p);
+            EQC_CHECK_LAUNCH();
+            count_launch();
+            h.ref_stage.download(out, h.nglob, h.stream);
         }
+        EQC_CUDA(cudaStreamSynchronize(h.stream));
     });
 }
 
@@ -648,9 +674,12 @@ eqc_status eqc_set_state(eqc_handle* H, const char* name, const double* in) {
         if (fault) {
             b->upload(in, h.F.Nf, h.stream);
         } else {
-            std::vector<double> l;
-            to_layout(h, in, l);
-            b->upload(l.data(), l.size(), h.stream);
+            ensure_ref_maps(h);
+            h.ref_stage.upload(in, h.nglob, h.stream);
+            b->zero(h.stream);
+            k_ref_to_layout<<<ref_blocks(h.nglob), 256, 0, h.stream>>>(h.ref_stage.p, h.d_ref2lay.p, h.nglob, b->p);
+            EQC_CHECK_LAUNCH();
+            count_launch();
         }
         invalidate_residual(h);
         EQC_CUDA(cudaStreamSynchronize(h.stream));

@@ -143,7 +143,8 @@ struct Handle {
     cudaStream_t side_stream = nullptr, side_stream2 = nullptr;
     bool pdl_off = false;        // the graph being captured holds that step: no programmatic edges
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
-    DBuf<int64_t> d_ref2lay;
+    DBuf<int> d_ref2lay;         // ref2lay on the device (eqc_get_state / eqc_set_state), and
+    DBuf<double> ref_stage;      // the field in the reference numbering on its way in or out
     // element data
     DBuf<double> W64, W64p;
     DBuf<float> W32, W32p;

@@ -180,9 +180,14 @@ class Solver:
         self._chk(L.lib().eqc_run(self.h, int(max_steps), float(t_end), C.byref(st)))
         return st.as_dict()
 
-    def state(self, name: str) -> np.ndarray:
+    def state(self, name: str, out: np.ndarray = None) -> np.ndarray:
+        """A state field in the reference numbering, into out when given (a C-contiguous float64
+        array of the field's length, e.g. in pinned host memory) or a new array."""
         n = self.nglob if name in ("d", "v", "a") else self.Nf
-        out = np.zeros(n)
+        if out is None:
+            out = np.zeros(n)
+        elif out.dtype != np.float64 or out.shape != (n,) or not out.flags.c_contiguous:
+            raise ValueError(f"state {name}: out must be a contiguous float64 array of length {n}")
         self._chk(L.lib().eqc_get_state(self.h, name.encode(), L.dptr(out)))
         return out
 
