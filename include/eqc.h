@@ -246,7 +246,10 @@ typedef struct {
 eqc_status eqc_run(eqc_handle* h, int64_t max_steps, double t_end, eqc_run_stats* stats);
 
 /* State on the host (reference numbering): name is one of "d", "v", "a"
- * [nglob], "psi", "tau" [FltNglob].  eqc_set_state writes it back. */
+ * [nglob], "psi", "tau" [FltNglob].  eqc_set_state writes it back.  The array
+ * crosses to or from the device as it is (page-locked host memory, e.g. from
+ * cudaHostAlloc, makes that one DMA) and is permuted on the device; both calls
+ * return when the transfer is complete. */
 eqc_status eqc_get_state(eqc_handle* h, const char* name, double* out);
 eqc_status eqc_set_state(eqc_handle* h, const char* name, const double* in);
 /* Scalars "t", "dt", "isolver", "it" (and, read-only, the solver counters "cg_iters",
