@@ -527,7 +527,8 @@ def bench_ours(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / max(st["steps"], 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic: seeded initial state of the damage-zone model (no dataset)",
-        "config": {"workload": f"{args.workload}: 480x240-element damage-zone model, 1,846,081 nodes, 961 fault "
+        "config": {"workload": f"{args.workload}: {'damage-zone' if P.cfg.damage else 'homogeneous'} model of "
+                               f"NelX x NelY = {P.cfg.NelX} x {P.cfg.NelY} elements, {nglob:,} nodes, {Nf:,} fault "
                                f"nodes; interseismic window after {args.warmup} warm-up steps from the steady-sliding "
                                f"start; mixed-precision multigrid-PCG (tol 1e-8), extrapolated initial guess, "
                                f"autotuned smoother",
