@@ -101,4 +101,26 @@ EQC_HD double df_widen(float f) {
 }
 EQC_HD double df_to_double(df x) { return df_widen(x.hi) + df_widen(x.lo); }
 
+#if defined(__CUDACC__)
+// x * 2^e (p2 = 2^e), exact: the exponent field moved by integer arithmetic where x and the
+// result are normal FP64 numbers, else the FP64 multiply (zeros, subnormals, infinities, NaNs,
+// a result out of the normal range).
+__device__ __forceinline__ double pow2_scale(double x, int e, double p2) {
+    const int64_t b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff), en = ex + e;
+    if (ex != 0 && ex != 0x7ff && en > 0 && en < 0x7ff) return __longlong_as_double(b + ((int64_t)e << 52));
+    return x * p2;
+}
+// FP64 -> FP32 through the double-float split (integer operations and one FP32 add) inside
+// df_from_double's range [2^-90, 2^120]: the nearest FP32 number but for the rare remainders that
+// round to a tie on the way (then one unit in the last place off).  Outside it (zeros, tiny and
+// huge values, infinities, NaNs) the hardware conversion, so those propagate as they should.
+__device__ __forceinline__ float f64_to_f32(double x) {
+    const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+    if (e < 1023 - 90 || e > 1023 + 120) return __double2float_rn(x);
+    const df d = df_from_double(x);
+    return __fadd_rn(d.hi, d.lo);
+}
+#endif
+
 }  // namespace eqc

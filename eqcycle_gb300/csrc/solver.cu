@@ -16,6 +16,7 @@
 #include "model.h"
 #include "reduce.cuh"
 #include "vec.cuh"
+#include "epi.cuh"
 #include <cmath>
 #include <cstddef>
 
@@ -135,10 +136,13 @@ __global__ void k_jacobi(const T* __restrict__ r, const T* __restrict__ dg, T* _
 // intermediate reliable update (S->upd_incr) also dx64 += y32: dx64 is sigma times x's change since
 // r64 was last exact, whose K dx updates the residual (in the recurrence's scaled units, so that
 // the steady-sliding start's 1e-25 m increments stay inside double-float's range).
+// The widening and the scaling use integer operations (f32_to_f64, pow2_scale): one FP64 add per
+// vector and node, the same bits as (double) y / sigma.
 __global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, float* __restrict__ y,
                                                       double* __restrict__ dx, int64_t n, const CGState* S) {
     EQC_GRID_WAIT();
     const double inv = 1.0 / S->sigma;
+    const int es = -ilogb(S->sigma);
     const bool incr = dx && S->upd_incr;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double xx[4], dd[4];
@@ -148,8 +152,9 @@ __global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, fl
         if (incr) ld4(dx + i, dd);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            xx[k] += (double)yy[k] * inv;
-            if (incr) dd[k] += (double)yy[k];
+            const double yw = f32_to_f64(yy[k]);
+            xx[k] += pow2_scale(yw, es, inv);
+            if (incr) dd[k] += yw;
         }
         st4(x + i, xx);
         if (incr) st4(dx + i, dd);
@@ -167,16 +172,20 @@ __global__ void k_dx_init(double* __restrict__ dx, const float* __restrict__ g, 
         dx[i] = keep ? (double)g[i] * sg : 0.0;
 }
 // [intermediate reliable update (kdx given and S->upd_incr): r64 += kdx / sigma, kdx the
-// double-float -K dx of the scaled change] ; r32 = (float) (sigma r64) ; S->rr = sigma^2 r64.r64
-// (kdx given: a reliable update's end; r64 is then exact for x, so dx64 = 0.)
+// double-float -K dx of the scaled change] ; r32 = (float) (sigma r64) ; S->rr = r32.r32 (the
+// scaled norm, of the FP32 residual: within 1e-7 of sigma^2 r64.r64)
+// (kdx given: a reliable update's end; r64 is then exact for x, so dx64 = 0.)  The scaling and
+// the rounding to FP32 use integer operations (pow2_scale, f64_to_f32) and the norm the FP32
+// compensated sum: GB300's FP64 rate is a small fraction of its FP32 and integer rates.
 __global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(double* __restrict__ r64, float* __restrict__ r32,
                                                              int64_t n, double* part, unsigned* count, CGState* S,
                                                              const double* __restrict__ kdx, double* __restrict__ dx) {
     EQC_GRID_WAIT();
     __shared__ double sh[32];
     const double sg = S->sigma;
+    const int es = ilogb(sg);
     const bool incr = kdx && S->upd_incr;
-    double s = 0.0;
+    DotAcc<float> acc;
     for (int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); i < n; i += 4 * (int64_t)gridDim.x * blockDim.x) {
         double v[4];
         float f[4];
@@ -195,13 +204,13 @@ __global__ void __launch_bounds__(VEC_THREADS) k_demote_norm(double* __restrict_
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            f[k] = (float)(v[k] * sg);
-            s += v[k] * v[k];
+            f[k] = f64_to_f32(pow2_scale(v[k], es, sg));
+            acc.add(f[k], f[k]);
         }
         st4(r32 + i, f);
     }
-    s = block_sum(s, sh);
-    finish_reduction(s, part, count, sh, [&](double t) { S->rr = t * sg * sg; });
+    const double s = block_sum(acc.value(), sh);
+    finish_reduction(s, part, count, sh, [&](double t) { S->rr = t; });
 }
 
 // Scale of the FP32 recurrence for this solve: sigma = 2^-e with 2^e <= ||b|| < 2^(e+1)

@@ -46,16 +46,23 @@ __global__ void k_qs_begin_bulk(double* __restrict__ d, double* __restrict__ dPr
     EQC_GRID_WAIT();
     const bool use = extrap && C->qs_prev && C->dt_prev > 0;
     const double ratio = use ? C->dt / C->dt_prev : 0.0;
+    const float ratio_f = (float)ratio;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double dn = d[i], dp = dPre[i];
         dPre[i] = dn;
         if (i >= ld) {
-            const double gi = use ? ratio * (dn - dp) : 0.0;
-            const float gf = (float)gi;
-            // round_g (mixed precision): the increment added is the FP32 one the solver accounts
-            // for (its intermediate reliable updates correct the residual by K of x's change)
-            d[i] = dn + (round_g ? (double)gf : gi);
-            g[i] = gf;
+            if (round_g) {
+                // mixed precision: the increment added is the FP32 one the solver accounts for (its
+                // intermediate reliable updates correct the residual by K of x's change), formed
+                // from the FP32-rounded difference (integer conversions: two FP64 operations)
+                const float gf = use ? __fmul_rn(ratio_f, f64_to_f32(dn - dp)) : 0.f;
+                if (use) d[i] = dn + f32_to_f64(gf);
+                g[i] = gf;
+            } else {
+                const double gi = use ? ratio * (dn - dp) : 0.0;
+                d[i] = dn + gi;
+                g[i] = (float)gi;
+            }
         } else {
             g[i] = 0.f;
         }
@@ -111,17 +118,18 @@ __global__ void __launch_bounds__(FNT) k_qs_end_fault(double* __restrict__ v, Fa
     }
 }
 
-// v[FltNI] = (d - dPre)/dt ; a = 0  (main.jl:289-292), rows >= 1
+// v[FltNI] = (d - dPre)/dt ; a = 0  (main.jl:289-292), rows >= 1; recip (mixed precision): times
+// 1/dt (an FP64 division is many FP64 operations, of which GB300 issues few)
 __global__ void k_qs_end_bulk(const double* __restrict__ d, const double* __restrict__ dPre, double* __restrict__ v,
-                              double* __restrict__ a, int64_t ld, int64_t n, Ctrl* C) {
+                              double* __restrict__ a, int64_t ld, int64_t n, Ctrl* C, int recip) {
     EQC_GRID_WAIT();
-    const double dt = C->dt;
+    const double dt = C->dt, inv = 1.0 / dt;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         C->kd_valid = 0;   // d changed: no incremental K d
         C->v_half = 0;     // v and a as the reference keeps them
     }
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if (i >= ld) v[i] = (d[i] - dPre[i]) / dt;
+        if (i >= ld) v[i] = recip ? (d[i] - dPre[i]) * inv : (d[i] - dPre[i]) / dt;
         a[i] = 0.;
     }
 }
@@ -876,7 +884,8 @@ static void enqueue_qs(Handle& h, bool graph) {
         count_launch();
     }
     k_qs_end_fault<<<fblocks(h.F.Nf), FNT, 0, s>>>(h.v.p, f, h.ctrl.p);
-    k_qs_end_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.a.p, L.ld, n, h.ctrl.p);
+    k_qs_end_bulk<<<vblocks(n), 256, 0, s>>>(h.d.p, h.dPre.p, h.v.p, h.a.p, L.ld, n, h.ctrl.p,
+                                             h.opt.precision == EQC_MIXED ? 1 : 0);
     count_launch(2);
     if (h.nCreep) {
         k_zero_list<<<1, 256, 0, s>>>(h.iCreep.p, h.nCreep, h.d.p, h.v.p, nullptr);
