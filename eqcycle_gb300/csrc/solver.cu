@@ -533,7 +533,7 @@ static void iter_mixed_a(Handle& h, double delta, cudaGraphConditionalHandle hi,
 // Reliable update: x += y ; r = b - K_II x in FP64 ; r32 = r ; S->rr = ||r||^2.
 // An intermediate update (the recurrence residual fell by the update factor and the loop goes on)
 // instead computes r -= K_II dx with the double-float apply of the correction dx folded since the
-// previous update (69 against 160 us on dz480): K dx has the size of the residual it corrects, so
+// previous update (69 against 139 us on dz480): K dx has the size of the residual it corrects, so
 // the double-float error stays far below the residual left.  The update that certifies
 // convergence recomputes b - K_II x with the FP64 apply: the full K x's double-float error would
 // floor the residual near 1e-5 of |b| late in a cycle (|K||x| / |b| large; measured).  Both
