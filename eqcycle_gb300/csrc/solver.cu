@@ -164,12 +164,14 @@ __global__ void __launch_bounds__(VEC_THREADS) k_fold(double* __restrict__ x, fl
 }
 
 // dx64 = sigma times the kept initial-guess increment (r64 is the residual without it), else 0.
+// (widening and the power-of-two scaling by integer operations: the bits of (double) g * sigma)
 __global__ void k_dx_init(double* __restrict__ dx, const float* __restrict__ g, const CGState* S, int64_t n) {
     EQC_GRID_WAIT();
     const bool keep = g && S->guess_keep;
     const double sg = S->sigma;
+    const int es = ilogb(sg);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        dx[i] = keep ? (double)g[i] * sg : 0.0;
+        dx[i] = keep ? pow2_scale(f32_to_f64(g[i]), es, sg) : 0.0;
 }
 // [intermediate reliable update (kdx given and S->upd_incr): r64 += kdx / sigma, kdx the
 // double-float -K dx of the scaled change] ; r32 = (float) (sigma r64) ; S->rr = r32.r32 (the

@@ -341,3 +341,31 @@ def test_mixed_dynamic_steps_match_oracle(eqclib, oracle_mod):
     for k in ("d", "v", "psi", "tau"):
         assert rel(got[k], ref[k]) <= 1e-6, k
     assert rel(res.Vfmax, o.get("Vfmax")) <= 1e-6
+
+
+def test_state_transfers_round_trip_through_pinned_buffers(eqclib):
+    """eqc_get_state / eqc_set_state permute node fields between the reference numbering and the
+    padded device layout on the device: reading into a caller's (pinned) array gives the same
+    bits as a fresh one, and writing a field back and reading it again returns it unchanged, on
+    a mesh whose rows carry padding."""
+    torch = pytest.importorskip("torch")
+    P = set_parameters(preset("homog48"))
+    with Solver(P, precision=EQC_MIXED, precond=EQC_PC_AMG) as s:
+        nx, ny, ld = s.layout()
+        assert ld > nx   # padded rows
+        s.init(P.cfg.V_init)
+        s.run(3)
+        rng = np.random.default_rng(5)
+        for name in ("d", "v", "a", "psi", "tau"):
+            x = s.state(name)
+            buf = torch.empty(x.size, dtype=torch.float64, pin_memory=True).numpy()
+            assert np.array_equal(s.state(name, out=buf), x), name
+            y = rng.standard_normal(x.size)
+            ybuf = torch.empty(x.size, dtype=torch.float64, pin_memory=True).numpy()
+            ybuf[:] = y
+            s.set_state(name, ybuf)
+            assert np.array_equal(s.state(name), y), name
+            s.set_state(name, x)
+            assert np.array_equal(s.state(name), x), name
+        with pytest.raises(ValueError):
+            s.state("d", out=np.zeros(3))
