@@ -2,8 +2,7 @@
 // the restriction and prolongation between levels, the Chebyshev steps and the dense coarse
 // solve's rows.  Every multiply-add is an explicit round-to-nearest FMA, so any kernel built from
 // these functions gives the same bits as the V-cycle's own.  Ld is the load of the vectors the
-// V-cycle writes (a kernel whose CTAs read what other CTAs wrote during the same launch would
-// pass one that bypasses L1).
+// V-cycle writes: plain (LdPlain) or with a pending Chebyshev direction added (LdPend).
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -111,29 +110,6 @@ __device__ __forceinline__ void cheb_first_step_pt(T* x, T* r, T* d, const T* b,
     r[i] = ri;
     d[i] = di;
     x[i] = with_x ? add_rn<T>(ld(x + i), di) : di;
-}
-
-// The epilogue of a stencil apply at point i (OpEpi modes 0-3), with the vectors it reads
-// loaded through ld.
-template <class T, class Ld>
-__device__ __forceinline__ void epi_store1_ld(const OpEpi<T>& E, T* y, int64_t i, T t, Ld ld) {
-    if (E.mode == 0) {
-        y[i] = t;
-    } else if (E.mode == 1) {
-        E.r[i] = sub_rn<T>(ld(E.b + i), t);
-    } else if (E.mode == 3) {
-        T r, d;
-        cheb_first_rd_pt<T>(r, d, ld(E.b + i), t, E.dinv[i], E.inv_theta);
-        E.r[i] = r;
-        E.dnew[i] = d;
-    } else {
-        T r = ld(E.r + i), d = ld(E.dold + i), x = ld(E.x + i);
-        if (E.x_pend) x = add_rn<T>(x, d);
-        cheb_step_pt<T>(r, d, x, t, E.dinv[i], E.c1, E.c2);
-        E.r[i] = r;
-        E.x[i] = x;
-        E.dnew[i] = d;
-    }
 }
 
 // One row of the coarsest level's dense inverse times b, by one warp: the lanes' partial sums
