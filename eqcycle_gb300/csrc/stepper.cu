@@ -769,11 +769,6 @@ __global__ void __launch_bounds__(FNT) k_init_psi(const double* v, FaultArgs f) 
         f.psi[k] = f.tauo[k] / (f.Seff[k] * f.ccb[k]) - f.fo[k] / f.ccb[k] -
                    (f.cca[k] / f.ccb[k]) * log(2 * v[k] / f.Vo[k]);
 }
-__global__ void k_fill(double* x, double val, int64_t n) {
-    EQC_GRID_WAIT();
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        x[i] = val;
-}
 // Fill value only on real nodes (row padding stays zero).
 __global__ void k_fill_nodes(double* x, double val, Layout L) {
     EQC_GRID_WAIT();
